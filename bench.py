@@ -1,0 +1,335 @@
+#!/usr/bin/env python3
+"""Benchmark: critical-curve points per second on one synthetic star field.
+
+Workload (default): 2000 Salpeter stars (m in [0.08, 1.5] solar masses,
+rescaled to mean 1), rectangular field, kappa_tot 0.45, kappa_star 0.35,
+shear 0.35, theta_star 1, num_phi 2048 (the nearest value the reference
+accepts for 2000: a multiple of 2 * num_branches), 32 branches -- 4056 roots,
+8.44e6 critical-curve points per field.
+
+A step is one full field solve: star generation, tree and FMM, the Aberth
+solve at every branch centre, the phi continuation, the 1/mu residual and
+the caustic map of every point, all resident in HBM.  ``value`` is points/s
+from the device-side span of each step (CUDA events in the library, star
+generation -> caustics on the device); ``e2e`` is the same metric through the
+public API with a host star array in and host result arrays (roots and
+caustics) out, timed around the calls.  L2 is flushed (256 MiB write) before
+every timed step.
+
+Multi-GPU: fields are independent, so N ranks run N replicas (seed + rank)
+with no collective on the data path ("scaling": "weak"); value is all ranks'
+points over the slowest rank's time.
+
+--impl reference times the reference algorithm on the host cores: the CPU
+restatement in oracle/ (the reference's own code cannot travel to this
+machine), on a bounded sample (the first branches for the first phi steps),
+extrapolated to the full field from its initial-solve and per-step timers.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "single_field_n2000_salpeter_rect": dict(
+        kappa_tot=0.45, kappa_star=0.35, shear=0.35, theta_star=1.0, mass_function="salpeter",
+        m_lower=0.08, m_upper=1.5, m_solar=4.954984, rectangular=1, approx=1, num_stars=2000,
+        num_phi=2048, num_branches=32, random_seed=1235),
+    "small_field_n100_equal_disc": dict(
+        kappa_tot=0.3, kappa_star=0.3, shear=0.1, theta_star=1.0, mass_function="equal", rectangular=0,
+        approx=1, num_stars=100, num_phi=100, num_branches=1, random_seed=1234),
+    "large_field_n20000_kroupa_rect": dict(
+        kappa_tot=0.7, kappa_star=0.6, shear=0.2, theta_star=1.0, mass_function="kroupa", m_lower=0.08,
+        m_upper=1.5, m_solar=1.0, rectangular=1, approx=1, num_stars=20000, num_phi=10240,
+        num_branches=128, random_seed=1236),
+}
+DEFAULT = "single_field_n2000_salpeter_rect"
+METRIC = "crit-curve pts/s mixed vs plain FP64 (err≤1e-9); fields/s, p50/p99 latency"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            if self.thread:
+                self.thread.join(timeout=2)
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measure_peaks() -> dict:
+    exe = os.path.join(ROOT, "ccf_gb300", "lib", "ccf_peaks")
+    try:
+        out = subprocess.run([exe], capture_output=True, text=True, timeout=120).stdout.strip().splitlines()[-1]
+        return json.loads(out)
+    except Exception as e:  # noqa: BLE001
+        return {"error": str(e)}
+
+
+def algorithmic_flops(info: dict, continuation_only: bool = True, n_near: int = 32) -> float:
+    """FP work of the executed Aberth updates: 10 flops per reciprocal-sum
+    term (complex difference 2, |d|^2 3, reciprocal 1, scale 2, accumulate 2)
+    plus 40 per near star, 16 per expansion order and 12 per Taylor term of
+    the smooth-mass series per update."""
+    terms, updates = info["sum_terms"], info["root_updates"]
+    if continuation_only:
+        terms -= info["sum_terms_init"]
+        updates -= info["root_updates_init"]
+    extra = 40 * n_near + 16 * info["expansion_order"] + (12 * (info["taylor_smooth"] - 1) if info["rectangular"] else 0)
+    return 10.0 * terms + float(extra) * updates
+
+
+def cpu_reference(cfg: dict, threads: int, branches: int | None = None, steps: int = 2) -> dict:
+    """Reference algorithm (CPU restatement) on a bounded sample, extrapolated."""
+    from oracle import oracle as O
+    nb = cfg["num_branches"]
+    half = cfg["num_phi"] // (2 * nb)
+    m = min(nb, branches or max(1, threads))
+    st = min(steps, half)
+    t0 = time.perf_counter()
+    r = O.run(num_threads=threads, max_branches=m, max_steps=st, **cfg)
+    wall = time.perf_counter() - t0
+    inf = r["info"]
+    t_full = inf["t_init_roots"] * (nb / m) + inf["t_ccs"] * (nb / m) * (half / st) + inf["t_caustics"] * (nb / m) * (half / st)
+    points = inf["num_roots"] * (cfg["num_phi"] + nb)
+    return {"value": points / t_full, "t_full_extrapolated": t_full, "sample_wall": wall,
+            "sample": f"{m} of {nb} branches, {st} of {half} phi steps per side, fixed 30/20 sweeps; "
+                      f"extrapolated linearly in branches and steps",
+            "cores": threads}
+
+
+def run_reference(args) -> None:
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    cfg = WORKLOADS[args.workload]
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_reference(cfg, threads, steps=1)
+    vals = []
+    for _ in range(args.steps):
+        vals.append(cpu_reference(cfg, threads, steps=2))
+    v = statistics.median([x["value"] for x in vals])
+    points = vals[0]["value"] * vals[0]["t_full_extrapolated"]
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "points/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * points / v, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded star field)",
+        "config": {"workload": args.workload, **cfg},
+        "cpu_baseline": {"value": v, "unit": "points/s", "cores": threads, "kind": "port",
+                         "sample": vals[0]["sample"]},
+        "e2e": {"value": v, "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=DEFAULT, choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--fp64-steps", type=int, default=1, help="plain-FP64 steps timed beside the main arm")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    ws, rank, local = dist_env()
+    import numpy as np
+    import torch
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from ccf_gb300 import CCF
+
+    cfg = dict(WORKLOADS[args.workload])
+    cfg["random_seed"] = cfg["random_seed"] + rank
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def make(prec):
+        c = CCF(**cfg)
+        c.precision = prec
+        c.device = local
+        c.write_mu_length_scales = 0
+        return c
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+
+    c = make(args.precision)
+    for _ in range(max(3, args.warmup)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        assert c.run(-1), c.last_error()
+    infos = []
+    barrier()
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            assert c.run(-1), c.last_error()
+            infos.append(c.info())
+        barrier()
+    t_dev = sum(i["t_total"] for i in infos)
+    if ws > 1:
+        t = torch.tensor([t_dev], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_dev = float(t.item())
+    info = infos[-1]
+    points = info["num_points"]
+    value = points * args.steps * ws / t_dev
+
+    # end to end through the public API: host star array in, host roots and caustics out
+    res = c.results()
+    stars_host = np.ascontiguousarray(res["stars"])
+    corner = complex(info["corner_x1"], info["corner_x2"])
+    e = make(args.precision)
+    e.set_stars(stars_host, info["rectangular"], corner, info["theta_star"])
+    rows = info["num_roots"] * cfg["num_branches"]
+    cols = cfg["num_phi"] // cfg["num_branches"] + 1
+    assert e.run(-1), e.last_error()
+    e.results(stars=False)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e.set_stars(stars_host, info["rectangular"], corner, info["theta_star"])
+        assert e.run(-1), e.last_error()
+        out = e.results(stars=False)
+    barrier()
+    t_e2e = time.perf_counter() - t0
+    h2d = stars_host.nbytes
+    d2h = out["ccs"].nbytes + out["caustics"].nbytes + out["errs"].nbytes
+
+    # roofline of the dominant kernel: the continuation solver launch
+    peaks = measure_peaks()
+    t_cont = statistics.median(i["t_ccs"] for i in infos)
+    cont_share = t_cont / statistics.median(i["t_total"] for i in infos)
+    flops = algorithmic_flops(info, continuation_only=True)
+    achieved = flops / t_cont / 1e12 if t_cont > 0 else 0.0
+    peak32 = peaks.get("fp32_tflops")
+
+    fp64 = None
+    if args.precision == "mixed" and args.fp64_steps > 0:
+        d = make("fp64")
+        assert d.run(-1), d.last_error()
+        tt = []
+        for _ in range(args.fp64_steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            assert d.run(-1), d.last_error()
+            tt.append(d.info()["t_total"])
+        fp64 = {"value": points / statistics.median(tt), "unit": "points/s",
+                "ms_per_step": 1e3 * statistics.median(tt)}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        cb = cpu_reference(cfg, threads, steps=2)
+        cpu = {"value": cb["value"], "unit": "points/s", "cores": threads, "kind": "port", "sample": cb["sample"]}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64 (FP32 correction sums, FP64 root function)" if args.precision == "mixed" else "f64",
+            "data": "synthetic (seeded star field)",
+            "config": {"workload": args.workload, **cfg, "precision": args.precision,
+                       "l2": "flushed before every timed step (256 MiB write)", "parallelism": f"replicas x{ws}"},
+            "e2e": {"value": points * args.steps * ws / t_e2e, "unit": "points/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
+                         "frac": (achieved / peak32) if peak32 else None, "traffic": None,
+                         "kernel": "solve_kernel (phi continuation)", "kernel_share_of_step": cont_share,
+                         "peak_source": "ccf_gb300/lib/ccf_peaks (FFMA chains, measured)",
+                         "fp64_peak_tflops": peaks.get("fp64_tflops")},
+            "fp64_plain": fp64,
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+            "gpu_launches": int(info["kernel_launches"]) * args.steps,
+            "detail": {"num_points": points, "num_roots": info["num_roots"], "tree_levels": info["tree_levels"],
+                       "expansion_order": info["expansion_order"], "max_error_1/mu": info["max_error"],
+                       "unconverged": info["unconverged"], "sweeps_init": info["max_sweeps_init"],
+                       "sweeps_step": info["max_sweeps_step"], "root_updates": info["root_updates"],
+                       "sum_terms": info["sum_terms"], "t_stars": info["t_stars"], "t_tree": info["t_tree"],
+                       "t_init_roots": info["t_init_roots"], "t_ccs": info["t_ccs"], "peaks": peaks},
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

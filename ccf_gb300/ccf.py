@@ -1,0 +1,223 @@
+"""Python mirror of the reference's operator API, the class CCF<T>
+(include/ccf.cuh:34-1289): the same public fields with the same defaults,
+``run(verbose) -> bool`` and ``save(verbose) -> bool``, backed by the C ABI
+of include/ccf_gb300.h (no computation happens in Python).
+
+Additions: ``precision`` ("mixed" or "fp64"), ``results()`` returning the
+outputs as numpy arrays in the reference's file layout, ``info()`` with the
+derived parameters and timings, ``set_stars()`` for an in-memory star field,
+and ``run_batch()`` to solve many fields in shared persistent launches.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+_FIELDS = {
+    # name: (default, kind) -- include/ccf.cuh:42-62
+    "kappa_tot": (0.3, float),
+    "shear": (0.3, float),
+    "kappa_star": (0.27, float),
+    "theta_star": (1.0, float),
+    "mass_function_str": ("equal", str),
+    "m_solar": (1.0, float),
+    "m_lower": (0.01, float),
+    "m_upper": (50.0, float),
+    "rectangular": (0, int),
+    "approx": (1, int),
+    "safety_scale": (1.37, float),
+    "num_stars": (137, int),
+    "starfile": ("", str),
+    "num_phi": (100, int),
+    "num_branches": (1, int),
+    "random_seed": (0, int),
+    "write_stars": (1, int),
+    "write_critical_curves": (1, int),
+    "write_caustics": (1, int),
+    "write_mu_length_scales": (0, int),
+    "outfile_prefix": ("./", str),
+}
+
+
+class CCFError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{_lib.STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+        self.message = message
+
+
+class CCF:
+    """Critical-curve and caustic finder for one star field."""
+
+    def __init__(self, **kw):
+        self._L = _lib.load()
+        self._h = ctypes.c_void_p()
+        rc = self._L.ccf_create(ctypes.byref(self._h))
+        if rc != 0:
+            raise CCFError(rc, "ccf_create failed")
+        for k, (v, _) in _FIELDS.items():
+            setattr(self, k, v)
+        self.precision = "mixed"
+        self.output_float = 0
+        self.max_iters_init = 300
+        self.max_iters_step = 60
+        self.exact_binomials = 0
+        self.device = 0
+        self._stars_keep = None
+        self.last_status = 0
+        for k, v in kw.items():
+            if k == "mass_function":
+                k = "mass_function_str"
+            if not hasattr(self, k):
+                raise AttributeError(k)
+            setattr(self, k, v)
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None) and self._h.value:
+                self._L.ccf_destroy(self._h)
+                self._h = ctypes.c_void_p()
+        except Exception:
+            pass
+
+    # ---- parameters ----
+    def _params(self) -> _lib.CcfParams:
+        p = _lib.CcfParams()
+        self._L.ccf_default_params(ctypes.byref(p))
+        for k, (_, kind) in _FIELDS.items():
+            v = getattr(self, k)
+            name = "mass_function" if k == "mass_function_str" else k
+            if kind is str:
+                setattr(p, name, str(v).encode())
+            else:
+                setattr(p, name, kind(v))
+        prec = self.precision
+        p.precision = _lib.PRECISION_MIXED if str(prec).lower() in ("mixed", "1") else _lib.PRECISION_FP64
+        p.output_float = int(self.output_float)
+        p.max_iters_init = int(self.max_iters_init)
+        p.max_iters_step = int(self.max_iters_step)
+        p.exact_binomials = int(self.exact_binomials)
+        p.device = int(self.device)
+        return p
+
+    def _push(self):
+        p = self._params()
+        rc = self._L.ccf_set_params(self._h, ctypes.byref(p))
+        if rc != 0:
+            raise CCFError(rc, self.last_error())
+
+    def set_stars(self, stars, rectangular: int, corner: complex, theta_star: float = 1.0):
+        """Use this star field ((N, 3) array of x1, x2, mass) instead of generating one."""
+        if stars is None:
+            self._L.ccf_set_stars(self._h, 0, None, 0, 0.0, 0.0, 1.0)
+            self._stars_keep = None
+            return
+        a = np.ascontiguousarray(stars, dtype=np.float64).reshape(-1, 3)
+        corner = complex(corner)
+        rc = self._L.ccf_set_stars(self._h, a.shape[0], a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                   int(rectangular), corner.real, corner.imag, float(theta_star))
+        if rc != 0:
+            raise CCFError(rc, self.last_error())
+        self._stars_keep = a
+
+    def last_error(self) -> str:
+        return self._L.ccf_last_error(self._h).decode()
+
+    # ---- the reference's API ----
+    def run(self, verbose: int = 0) -> bool:
+        """CCF<T>::run (include/ccf.cuh:1265-1280)."""
+        self._push()
+        self.last_status = self._L.ccf_run(self._h, int(verbose))
+        if self.last_status == 0:
+            self.random_seed = self.info()["random_seed"] or self.random_seed
+        elif verbose >= 0:
+            import sys
+            sys.stderr.write(self.last_error() + "\n")
+        return self.last_status == 0
+
+    def save(self, verbose: int = 0) -> bool:
+        """CCF<T>::save (include/ccf.cuh:1282-1287)."""
+        self._push()
+        self.last_status = self._L.ccf_save(self._h, int(verbose))
+        if self.last_status != 0 and verbose >= 0:
+            import sys
+            sys.stderr.write(self.last_error() + "\n")
+        return self.last_status == 0
+
+    # ---- results ----
+    def info(self) -> dict:
+        i = _lib.CcfInfo()
+        self._L.ccf_get_info(self._h, ctypes.byref(i))
+        return i.as_dict()
+
+    def results(self, stars: bool = True) -> dict:
+        """Outputs in the reference's file layout: rows = num_roots * num_branches,
+        cols = num_phi / num_branches + 1, row = root * num_branches + branch."""
+        inf = self.info()
+        rows = inf["num_roots"] * self.num_branches
+        cols = self.num_phi // self.num_branches + 1
+        ccs = np.empty((rows, cols), dtype=np.complex128)
+        errs = np.empty((rows, cols))
+        caus = np.empty((rows, cols), dtype=np.complex128) if self.write_caustics else None
+        mu = np.empty((rows, cols)) if self.write_mu_length_scales else None
+        st = np.empty((inf["num_stars"], 3)) if stars else None
+        dp = lambda a: None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+        rc = self._L.ccf_get_results(self._h, dp(ccs), dp(caus), dp(errs), dp(mu), dp(st))
+        if rc != 0:
+            raise CCFError(rc, self.last_error())
+        return {"ccs": ccs, "caustics": caus, "errs": errs, "mu_length_scales": mu, "stars": st, "info": inf}
+
+
+    def eval_points(self, z, phi) -> dict:
+        """f, df/dz, lens map, 1/mu bound and length scale at points z (after run)."""
+        z = np.ascontiguousarray(z, dtype=np.complex128).ravel()
+        phi = np.ascontiguousarray(np.broadcast_to(phi, z.shape), dtype=np.float64)
+        out = {"f": np.empty_like(z), "df": np.empty_like(z), "w": np.empty_like(z),
+               "err": np.empty(z.shape), "mu_length": np.empty(z.shape)}
+        dp = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+        rc = self._L.ccf_eval_points(self._h, z.shape[0], dp(z.view(np.float64)), dp(phi), dp(out["f"].view(np.float64)),
+                                     dp(out["df"].view(np.float64)), dp(out["w"].view(np.float64)), dp(out["err"]),
+                                     dp(out["mu_length"]))
+        if rc != 0:
+            raise CCFError(rc, self.last_error())
+        return out
+
+
+def run_batch(fields: list[CCF], verbose: int = 0) -> bool:
+    """Solve several fields in shared solver launches (one initial-solve and
+    one continuation launch for the whole batch)."""
+    if not fields:
+        return True
+    L = fields[0]._L
+    for f in fields:
+        f._push()
+    arr = (ctypes.c_void_p * len(fields))(*[f._h.value for f in fields])
+    rc = L.ccf_run_batch(arr, len(fields), int(verbose))
+    for f in fields:
+        f.last_status = rc
+    return rc == 0
+
+
+def derive_params(**kw) -> dict:
+    """Checks and derived parameters on the host (no GPU needed)."""
+    c = CCF.__new__(CCF)
+    c._L = _lib.load()
+    for k, (v, _) in _FIELDS.items():
+        setattr(c, k, v)
+    c.precision, c.output_float, c.max_iters_init, c.max_iters_step, c.exact_binomials, c.device = \
+        "mixed", 0, 300, 60, 0, 0
+    for k, v in kw.items():
+        if k == "mass_function":
+            k = "mass_function_str"
+        setattr(c, k, v)
+    p = c._params()
+    info = _lib.CcfInfo()
+    msg = ctypes.create_string_buffer(512)
+    rc = c._L.ccf_derive_params(ctypes.byref(p), ctypes.byref(info), msg, 512)
+    d = info.as_dict()
+    d["rc"] = rc
+    d["error"] = msg.value.decode()
+    return d

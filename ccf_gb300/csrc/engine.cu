@@ -1,0 +1,809 @@
+/******************************************************************************
+engine.cu -- host orchestration of the device pipeline.
+
+Per field (CCF<T>::run, include/ccf.cuh:1265-1280):
+  stars      generate (or upload) the star field, star statistics, corner
+             update (include/ccf.cuh:602-730)
+  tree       level-by-level split with one small device->host read per level
+             (include/ccf.cuh:732-838)
+  fmm        expansion order, binomial table, upward and downward passes,
+             leaf records (include/ccf.cuh:840-901)
+Per batch of fields:
+  solve      one initial-solve launch over every branch centre of every
+             field, one continuation launch over every (branch, side) row;
+             residual, caustics and length scales come out of the solver
+             epilogues (include/ccf.cuh:906-1121)
+The engine never resets the device and reuses its buffers across runs.
+******************************************************************************/
+#include "engine.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <iostream>
+#include <numeric>
+
+namespace ccf
+{
+
+#define CCF_TRY(expr, what)                              \
+	do                                                   \
+	{                                                    \
+		cudaError_t _e = (expr);                         \
+		if (_e != cudaSuccess) return cuda_fail(_e, what); \
+	} while (0)
+
+Field::~Field()
+{
+	if (events)
+	{
+		for (auto& e : ev) cudaEventDestroy(e);
+	}
+}
+
+TreeDev Field::tree_dev() const
+{
+	TreeDev T;
+	T.center = n_center.ptr;
+	T.half = n_half.ptr;
+	T.level = n_level.ptr;
+	T.parent = n_parent.ptr;
+	T.child = n_child.ptr;
+	T.star_start = n_sstart.ptr;
+	T.star_count = n_scount.ptr;
+	T.nbr = n_nbr.ptr;
+	T.nbr_count = n_nbrc.ptr;
+	T.m2l = n_m2l.ptr;
+	T.m2l_count = n_m2lc.ptr;
+	T.p2l = n_p2l.ptr;
+	T.p2l_count = n_p2lc.ptr;
+	T.flag = n_flag.ptr;
+	T.rank = n_rank.ptr;
+	return T;
+}
+
+Engine::Engine() {}
+
+Engine::~Engine()
+{
+	if (stream) cudaStreamDestroy(stream);
+}
+
+ccf_status Engine::cuda_fail(cudaError_t e, const char* what)
+{
+	error = std::string("CUDA error check for ") + what + " failed: " + cudaGetErrorString(e);
+	cudaGetLastError();
+	return e == cudaErrorMemoryAllocation ? CCF_ERR_OUT_OF_MEMORY : CCF_ERR_CUDA;
+}
+
+bool Engine::ensure_device(int dev)
+{
+	if (initialized && dev == device) return true;
+	int n = 0;
+	cudaError_t e = cudaGetDeviceCount(&n);
+	if (e != cudaSuccess || n < 1)
+	{
+		cudaGetLastError();
+		error = "Error. No CUDA capable devices detected.";
+		return false;
+	}
+	if (dev < 0 || dev >= n)
+	{
+		error = "Error. Invalid CUDA device " + std::to_string(dev);
+		return false;
+	}
+	if (cudaSetDevice(dev) != cudaSuccess)
+	{
+		error = "Error. cudaSetDevice failed";
+		return false;
+	}
+	if (stream)
+	{
+		cudaStreamDestroy(stream);
+		stream = nullptr;
+	}
+	if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess)
+	{
+		error = "Error. cudaStreamCreate failed";
+		return false;
+	}
+	cudaDeviceProp prop;
+	cudaGetDeviceProperties(&prop, dev);
+	num_sms = prop.multiProcessorCount;
+	slots_per_sm = std::min(solver_blocks_per_sm(true), solver_blocks_per_sm(false));
+	device = dev;
+	initialized = true;
+	return true;
+}
+
+static void ensure_events(Field& f)
+{
+	if (f.events) return;
+	for (auto& e : f.ev) cudaEventCreate(&e);
+	f.events = true;
+}
+
+static float ev_ms(cudaEvent_t a, cudaEvent_t b)
+{
+	float ms = 0;
+	cudaEventElapsedTime(&ms, a, b);
+	return ms;
+}
+
+ccf_status Engine::prepare_field(Field& f, int verbose)
+{
+	ccf_params& p = f.params;
+	std::string msg;
+	std::unique_ptr<StarField> file_stars;
+	const StarField* sf = f.user_stars.get();
+	if (!sf && p.starfile[0])
+	{
+		file_stars.reset(new StarField());
+		if (!read_star_file(p.starfile, *file_stars, msg))
+		{
+			error = msg + "\nError. Unable to read star field parameters from file " + std::string(p.starfile);
+			return CCF_ERR_IO;
+		}
+		sf = file_stars.get();
+	}
+	if (!derive_params(p, sf, f.d, msg))
+	{
+		error = msg;
+		return CCF_ERR_INVALID_ARGUMENT;
+	}
+	Derived& d = f.d;
+	if (!d.star_input)
+	{
+		/* include/ccf.cuh:619-622 */
+		while (d.random_seed == 0)
+		{
+			d.random_seed = static_cast<int>(std::chrono::system_clock::now().time_since_epoch().count());
+		}
+		p.random_seed = d.random_seed;
+	}
+	if (verbose >= 2 && sf && d.kappa_star > p.kappa_tot) std::cerr << "Warning. kappa_star > kappa_tot\n";
+	const int N = d.num_stars;
+	cudaStream_t s = stream;
+	ensure_events(f);
+	CCF_TRY(cudaEventRecord(f.ev[0], s), "event");
+
+	CCF_TRY(f.star_gen.ensure(N), "cudaMalloc(stars)");
+	CCF_TRY(f.star_pos.ensure(N), "cudaMalloc(stars)");
+	CCF_TRY(f.star_tmp_pos.ensure(N), "cudaMalloc(stars)");
+	CCF_TRY(f.star_mass.ensure(N), "cudaMalloc(stars)");
+	CCF_TRY(f.star_tmp_mass.ensure(N), "cudaMalloc(stars)");
+	CCF_TRY(f.stats5.ensure(8), "cudaMalloc(stats)");
+	if (verbose >= 1 && !d.star_input) std::cout << "Generating star field...\n";
+	if (d.star_input)
+	{
+		std::vector<double2> pos(N);
+		std::vector<double> mass(N);
+		for (int i = 0; i < N; i++)
+		{
+			pos[i] = make_double2(sf->xym[3 * i], sf->xym[3 * i + 1]);
+			mass[i] = sf->xym[3 * i + 2];
+		}
+		CCF_TRY(cudaMemcpyAsync(f.star_gen.ptr, pos.data(), N * sizeof(double2), cudaMemcpyHostToDevice, s), "upload stars");
+		CCF_TRY(cudaMemcpyAsync(f.star_mass.ptr, mass.data(), N * sizeof(double), cudaMemcpyHostToDevice, s), "upload stars");
+		CCF_TRY(cudaStreamSynchronize(s), "upload stars");
+	}
+	else
+	{
+		MassTable mt = make_mass_table(d.mass_kind, d.m_lower, d.m_upper, p.m_solar);
+		launch_generate_stars(s, N, d.random_seed, d.rectangular, make_double2(d.corner_x1, d.corner_x2),
+			std::hypot(d.corner_x1, d.corner_x2), mt, f.star_gen.ptr, f.star_mass.ptr);
+		CCF_TRY(cudaGetLastError(), "generate_stars_kernel");
+	}
+	CCF_TRY(cudaMemcpyAsync(f.star_pos.ptr, f.star_gen.ptr, N * sizeof(double2), cudaMemcpyDeviceToDevice, s), "copy stars");
+	launch_star_stats(s, N, f.star_mass.ptr, f.stats5.ptr);
+	double st[5];
+	CCF_TRY(cudaMemcpyAsync(st, f.stats5.ptr, 5 * sizeof(double), cudaMemcpyDeviceToHost, s), "star stats");
+	CCF_TRY(cudaStreamSynchronize(s), "star stats");
+
+	/* include/star.cuh:124-161 and include/ccf.cuh:676-700 */
+	ccf_info& info = f.info;
+	std::memset(&info, 0, sizeof(info));
+	info.m_lower_actual = st[3];
+	info.m_upper_actual = st[4];
+	info.mean_mass_actual = st[0] / N;
+	info.mean_mass2_actual = st[1] / N;
+	info.mean_mass2_ln_mass_actual = st[2] / N;
+	if (d.rectangular) info.kappa_star_actual = st[0] * M_PI * d.theta * d.theta / (4 * d.corner_x1 * d.corner_x2);
+	else
+	{
+		double a = std::hypot(d.corner_x1, d.corner_x2);
+		info.kappa_star_actual = st[0] * d.theta * d.theta / (a * a);
+	}
+	update_corner(p, d, info.mean_mass_actual);
+	CCF_TRY(cudaEventRecord(f.ev[1], s), "event");
+	if (verbose >= 1) std::cout << "Done generating star field.\n";
+
+	if (verbose >= 1) std::cout << "Creating children and sorting stars...\n";
+	ccf_status rc = build_tree(f);
+	if (rc != CCF_OK) return rc;
+	rc = build_fmm(f);
+	if (rc != CCF_OK) return rc;
+	CCF_TRY(cudaEventRecord(f.ev[2], s), "event");
+	if (verbose >= 1) std::cout << "Done calculating multipole and local coefficients.\n";
+
+	/* outputs */
+	const int R = d.num_roots, nb = p.num_branches, cols = p.num_phi / nb + 1;
+	const size_t npts = (size_t)R * nb * cols;
+	CCF_TRY(f.ccs.ensure(npts), "cudaMalloc(ccs)");
+	CCF_TRY(f.errs.ensure(npts), "cudaMalloc(errs)");
+	if (p.write_caustics) CCF_TRY(f.caustics.ensure(npts), "cudaMalloc(caustics)");
+	if (p.write_mu_length_scales) CCF_TRY(f.mu.ensure(npts), "cudaMalloc(mu_length_scales)");
+	CCF_TRY(f.stats.ensure(16), "cudaMalloc(stats)");
+	CCF_TRY(cudaMemsetAsync(f.stats.ptr, 0, 16 * sizeof(unsigned long long), s), "memset");
+	if (p.precision == CCF_PRECISION_MIXED)
+	{
+		CCF_TRY(f.star_hilo.ensure(N), "cudaMalloc(star hilo)");
+		launch_star_hilo(s, N, f.star_pos.ptr, f.star_hilo.ptr);
+	}
+
+	/* info */
+	info.num_stars = N;
+	info.num_roots = R;
+	info.taylor_smooth = d.taylor_smooth;
+	info.rectangular = d.rectangular;
+	info.random_seed = d.star_input ? 0 : d.random_seed;
+	info.kappa_star = d.kappa_star;
+	info.theta_star = d.theta;
+	info.corner_x1 = d.corner_x1;
+	info.corner_x2 = d.corner_x2;
+	info.mu_ave = d.mu_ave;
+	info.alpha_error = d.alpha_error;
+	info.mean_mass = d.mean_mass;
+	info.mean_mass2 = d.mean_mass2;
+	info.mean_mass2_ln_mass = d.mean_mass2_ln_mass;
+	info.m_lower = d.m_lower;
+	info.m_upper = d.m_upper;
+	info.num_points = (long long)R * (p.num_phi + nb);
+	info.tree_levels = (int)f.level_start.size() - 1;
+	info.num_nodes = f.num_nodes;
+	info.num_leaves = f.num_leaves;
+	info.expansion_order = f.view.order;
+	/* kernels launched so far: star field (generate, statistics, FP32 split),
+	   tree (root, one flag pass per level, scan/children/partition/neighbours
+	   per split level), FMM (upward per level, downward from level 2, leaf
+	   flags, scan, leaf records) */
+	const int lv = info.tree_levels;
+	info.kernel_launches = (d.star_input ? 0 : 1) + 1 + (p.precision == CCF_PRECISION_MIXED ? 1 : 0) + 1 + (lv + 1) + 4 * lv
+		+ (lv + 1) + std::max(0, lv - 1) + 3;
+	return CCF_OK;
+}
+
+ccf_status Engine::build_tree(Field& f)
+{
+	cudaStream_t s = stream;
+	const int N = f.d.num_stars;
+	double rhl = f.d.rectangular ? std::max(f.d.corner_x1, f.d.corner_x2) : std::hypot(f.d.corner_x1, f.d.corner_x2);
+	rhl = rhl * 1.1;   /* include/ccf.cuh:746 */
+	f.info.root_half_length = rhl;
+
+	auto alloc_nodes = [&](int cap, int keep) -> cudaError_t {
+		cudaError_t e;
+		if ((e = f.n_center.grow(cap, keep, s)) != cudaSuccess) return e;
+		if ((e = f.n_half.grow(cap, keep, s)) != cudaSuccess) return e;
+		if ((e = f.n_level.grow(cap, keep, s)) != cudaSuccess) return e;
+		if ((e = f.n_parent.grow(cap, keep, s)) != cudaSuccess) return e;
+		if ((e = f.n_child.grow(cap, keep, s)) != cudaSuccess) return e;
+		if ((e = f.n_sstart.grow(cap, keep, s)) != cudaSuccess) return e;
+		if ((e = f.n_scount.grow(cap, keep, s)) != cudaSuccess) return e;
+		if ((e = f.n_nbr.grow((size_t)cap * MAX_NBR, (size_t)keep * MAX_NBR, s)) != cudaSuccess) return e;
+		if ((e = f.n_nbrc.grow(cap, keep, s)) != cudaSuccess) return e;
+		if ((e = f.n_m2l.grow((size_t)cap * MAX_M2L, (size_t)keep * MAX_M2L, s)) != cudaSuccess) return e;
+		if ((e = f.n_m2lc.grow(cap, keep, s)) != cudaSuccess) return e;
+		if ((e = f.n_p2l.grow((size_t)cap * MAX_P2L, (size_t)keep * MAX_P2L, s)) != cudaSuccess) return e;
+		if ((e = f.n_p2lc.grow(cap, keep, s)) != cudaSuccess) return e;
+		if ((e = f.n_flag.grow(cap, keep, s)) != cudaSuccess) return e;
+		if ((e = f.n_rank.grow(cap, keep, s)) != cudaSuccess) return e;
+		f.node_cap = cap;
+		return cudaSuccess;
+	};
+	int cap = std::max(1024, 2 * N + 64);
+	if (f.node_cap < cap) CCF_TRY(alloc_nodes(cap, 0), "cudaMalloc(tree)");
+	CCF_TRY(f.level_out.ensure(4), "cudaMalloc(tree)");
+	f.level_start.assign(1, 0);
+	f.level_count.assign(1, 1);
+	launch_tree_root(s, f.tree_dev(), rhl, N);
+	CCF_TRY(cudaMemsetAsync(f.level_out.ptr, 0, 4 * sizeof(int), s), "memset");
+	int L = 0;
+	while (true)
+	{
+		int start = f.level_start[L], count = f.level_count[L];
+		CCF_TRY(cudaMemsetAsync(f.level_out.ptr, 0, 2 * sizeof(int), s), "memset");
+		launch_tree_flag(s, f.tree_dev(), start, count, f.level_out.ptr);
+		int hv[3];
+		CCF_TRY(cudaMemcpyAsync(hv, f.level_out.ptr, 3 * sizeof(int), cudaMemcpyDeviceToHost, s), "tree level");
+		CCF_TRY(cudaStreamSynchronize(s), "get_node_star_info");
+		if (hv[2]) { error = "Error. Tree neighbour list overflow."; return CCF_ERR_NUMERIC; }
+		if (hv[0] <= MAX_NEAR) break;
+		int nflag = hv[1];
+		int child_start = start + count;
+		int need = child_start + 4 * nflag;
+		if (need > f.node_cap) CCF_TRY(alloc_nodes(std::max(need, 2 * f.node_cap), child_start), "cudaMalloc(tree)");
+		TreeDev T = f.tree_dev();
+		launch_scan(s, T.flag + start, T.rank + start, count);
+		launch_tree_children(s, T, start, count, child_start);
+		launch_tree_partition(s, T, start, count, f.star_pos.ptr, f.star_mass.ptr, f.star_tmp_pos.ptr, f.star_tmp_mass.ptr);
+		launch_tree_neighbors(s, T, child_start, 4 * nflag, f.level_out.ptr + 2);
+		CCF_TRY(cudaGetLastError(), "tree kernels");
+		f.level_start.push_back(child_start);
+		f.level_count.push_back(4 * nflag);
+		L++;
+		if (L > 40) { error = "Error. Tree deeper than 40 levels."; return CCF_ERR_NUMERIC; }
+	}
+	f.num_nodes = f.level_start[L] + f.level_count[L];
+	return CCF_OK;
+}
+
+ccf_status Engine::build_fmm(Field& f)
+{
+	cudaStream_t s = stream;
+	ccf_params& p = f.params;
+	Derived& d = f.d;
+	const int levels = (int)f.level_start.size() - 1;
+	const double rhl = f.info.root_half_length;
+	/* include/ccf.cuh:840-852 */
+	int P = (int)std::ceil(2 * std::log2(d.theta) + levels - std::log2(rhl) - std::log2(d.alpha_error));
+	if (P < 3) { error = "Error. Expansion order needs to be >= 3"; return CCF_ERR_INVALID_ARGUMENT; }
+	if (P > MAX_ORDER) { error = "Error. Maximum allowed expansion order is " + std::to_string(MAX_ORDER); return CCF_ERR_INVALID_ARGUMENT; }
+	std::vector<double> B = binomial_table(2 * P, !p.exact_binomials);
+	CCF_TRY(f.binom.ensure(B.size()), "cudaMalloc(binomials)");
+	CCF_TRY(cudaMemcpyAsync(f.binom.ptr, B.data(), B.size() * sizeof(double), cudaMemcpyHostToDevice, s), "binomials");
+	const size_t nc = (size_t)f.num_nodes * (P + 1);
+	CCF_TRY(f.multi.ensure(nc), "cudaMalloc(multipole)");
+	CCF_TRY(f.local.ensure(nc), "cudaMalloc(local)");
+	CCF_TRY(cudaMemsetAsync(f.multi.ptr, 0, nc * sizeof(double2), s), "memset");
+	CCF_TRY(cudaMemsetAsync(f.local.ptr, 0, nc * sizeof(double2), s), "memset");
+	TreeDev T = f.tree_dev();
+	for (int L = levels; L >= 0; L--)
+	{
+		launch_fmm_upward(s, T, f.level_start[L], f.level_count[L], P, f.star_pos.ptr, f.star_mass.ptr, f.multi.ptr, f.binom.ptr);
+	}
+	for (int L = 2; L <= levels; L++)
+	{
+		launch_fmm_downward(s, T, f.level_start[L], f.level_count[L], P, f.star_pos.ptr, f.star_mass.ptr, f.multi.ptr,
+			f.local.ptr, f.binom.ptr);
+	}
+	CCF_TRY(cudaGetLastError(), "fmm kernels");
+
+	/* leaves */
+	CCF_TRY(f.leaf_flag.ensure(f.num_nodes), "cudaMalloc(leaves)");
+	CCF_TRY(f.leaf_index.ensure(f.num_nodes), "cudaMalloc(leaves)");
+	CCF_TRY(f.node_leaf.ensure(f.num_nodes), "cudaMalloc(leaves)");
+	launch_leaf_flag(s, T, f.num_nodes, f.leaf_flag.ptr);
+	launch_scan(s, f.leaf_flag.ptr, f.leaf_index.ptr, f.num_nodes);
+	int tail[2];
+	CCF_TRY(cudaMemcpyAsync(&tail[0], f.leaf_index.ptr + f.num_nodes - 1, sizeof(int), cudaMemcpyDeviceToHost, s), "leaves");
+	CCF_TRY(cudaMemcpyAsync(&tail[1], f.leaf_flag.ptr + f.num_nodes - 1, sizeof(int), cudaMemcpyDeviceToHost, s), "leaves");
+	CCF_TRY(cudaStreamSynchronize(s), "leaves");
+	const int nl = tail[0] + tail[1];
+	f.num_leaves = nl;
+	CCF_TRY(f.leaf_center.ensure(nl), "cudaMalloc(leaves)");
+	CCF_TRY(f.leaf_inv_half.ensure(nl), "cudaMalloc(leaves)");
+	CCF_TRY(f.leaf_near_count.ensure(nl), "cudaMalloc(leaves)");
+	CCF_TRY(f.leaf_near.ensure((size_t)nl * MAX_NEAR), "cudaMalloc(leaves)");
+	CCF_TRY(f.leaf_loc.ensure((size_t)nl * 3 * (P + 1)), "cudaMalloc(leaves)");
+	CCF_TRY(f.leaf_loc3f.ensure((size_t)nl * (P + 1)), "cudaMalloc(leaves)");
+	CCF_TRY(cudaMemsetAsync(f.level_out.ptr + 2, 0, sizeof(int), s), "memset");
+	launch_leaf_build(s, T, f.num_nodes, f.leaf_index.ptr, P, d.theta * d.theta, f.star_pos.ptr, f.star_mass.ptr, f.local.ptr,
+		f.leaf_center.ptr, f.leaf_inv_half.ptr, f.leaf_near_count.ptr, f.leaf_near.ptr, f.leaf_loc.ptr, f.leaf_loc3f.ptr,
+		f.node_leaf.ptr, f.level_out.ptr + 2);
+	CCF_TRY(cudaGetLastError(), "leaf_build_kernel");
+
+	/* smooth-mass polynomials */
+	SmoothPoly sp = smooth_polynomials(d.kappa_star, d.corner_x1, d.corner_x2, d.taylor_smooth);
+	{
+		std::vector<double2> d1(std::max(1, sp.m)), d2(std::max(1, sp.m)), a(sp.a.size());
+		std::vector<float2> d2f(std::max(1, sp.m));
+		for (int i = 0; i < sp.m; i++)
+		{
+			d1[i] = make_double2(sp.d1[i].real(), sp.d1[i].imag());
+			d2[i] = make_double2(sp.d2[i].real(), sp.d2[i].imag());
+			d2f[i] = make_float2((float)sp.d2[i].real(), (float)sp.d2[i].imag());
+		}
+		for (size_t i = 0; i < a.size(); i++) a[i] = make_double2(sp.a[i].real(), sp.a[i].imag());
+		CCF_TRY(f.sm_d1.ensure(d1.size()), "cudaMalloc(smooth)");
+		CCF_TRY(f.sm_d2.ensure(d2.size()), "cudaMalloc(smooth)");
+		CCF_TRY(f.sm_d2f.ensure(d2f.size()), "cudaMalloc(smooth)");
+		CCF_TRY(f.sm_a.ensure(a.size()), "cudaMalloc(smooth)");
+		CCF_TRY(cudaMemcpyAsync(f.sm_d1.ptr, d1.data(), d1.size() * sizeof(double2), cudaMemcpyHostToDevice, s), "smooth");
+		CCF_TRY(cudaMemcpyAsync(f.sm_d2.ptr, d2.data(), d2.size() * sizeof(double2), cudaMemcpyHostToDevice, s), "smooth");
+		CCF_TRY(cudaMemcpyAsync(f.sm_d2f.ptr, d2f.data(), d2f.size() * sizeof(float2), cudaMemcpyHostToDevice, s), "smooth");
+		CCF_TRY(cudaMemcpyAsync(f.sm_a.ptr, a.data(), a.size() * sizeof(double2), cudaMemcpyHostToDevice, s), "smooth");
+		CCF_TRY(cudaStreamSynchronize(s), "smooth");
+	}
+	int lerr = 0;
+	CCF_TRY(cudaMemcpyAsync(&lerr, f.level_out.ptr + 2, sizeof(int), cudaMemcpyDeviceToHost, s), "leaves");
+	CCF_TRY(cudaStreamSynchronize(s), "leaves");
+	if (lerr) { error = "Error. A leaf has more than 32 near stars."; return CCF_ERR_NUMERIC; }
+
+	FieldView& V = f.view;
+	std::memset(&V, 0, sizeof(V));
+	V.kappa_tot = p.kappa_tot;
+	V.shear = p.shear;
+	V.kappa_star = d.kappa_star;
+	V.theta = d.theta;
+	V.theta2 = d.theta * d.theta;
+	V.rectangular = d.rectangular;
+	V.approx = p.approx;
+	V.taylor_smooth = d.taylor_smooth;
+	V.order = P;
+	V.num_roots = d.num_roots;
+	V.corner = make_double2(d.corner_x1, d.corner_x2);
+	V.corner_abs = std::hypot(d.corner_x1, d.corner_x2);
+	V.smooth_m = sp.m;
+	V.inv_corner = make_double2(sp.inv_corner.real(), sp.inv_corner.imag());
+	V.inv_corner2 = make_double2(sp.inv_corner2.real(), sp.inv_corner2.imag());
+	V.smooth_k1 = sp.k1;
+	V.smooth_d1 = f.sm_d1.ptr;
+	V.smooth_d2 = f.sm_d2.ptr;
+	V.smooth_a = f.sm_a.ptr;
+	V.smooth_d2f = f.sm_d2f.ptr;
+	V.num_stars = d.num_stars;
+	V.star_pos = f.star_pos.ptr;
+	V.star_mass = f.star_mass.ptr;
+	V.num_nodes = f.num_nodes;
+	V.node_center = f.n_center.ptr;
+	V.node_half = f.n_half.ptr;
+	V.node_child = f.n_child.ptr;
+	V.node_leaf = f.node_leaf.ptr;
+	V.num_leaves = nl;
+	V.leaf_center = f.leaf_center.ptr;
+	V.leaf_inv_half = f.leaf_inv_half.ptr;
+	V.leaf_near_count = f.leaf_near_count.ptr;
+	V.leaf_near = f.leaf_near.ptr;
+	V.leaf_loc = f.leaf_loc.ptr;
+	V.leaf_loc3f = f.leaf_loc3f.ptr;
+	CCF_TRY(f.view_dev.ensure(1), "cudaMalloc(view)");
+	CCF_TRY(cudaMemcpyAsync(f.view_dev.ptr, &V, sizeof(V), cudaMemcpyHostToDevice, s), "view");
+	return CCF_OK;
+}
+
+ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
+{
+	cudaStream_t s = stream;
+	const int nf = (int)fields.size();
+	const bool mixed = fields[0]->params.precision == CCF_PRECISION_MIXED;
+	for (Field* f : fields)
+	{
+		if ((f->params.precision == CCF_PRECISION_MIXED) != mixed)
+		{
+			error = "Error. All fields of a batch must use the same precision.";
+			return CCF_ERR_INVALID_ARGUMENT;
+		}
+	}
+	/* row offsets */
+	std::vector<long long> init_off(nf), cont_off(nf);
+	long long ninit = 0, ncont = 0;
+	int rows_init = 0, rows_cont = 0, minR = 1 << 30;
+	for (int i = 0; i < nf; i++)
+	{
+		const int R = fields[i]->d.num_roots, nb = fields[i]->params.num_branches;
+		init_off[i] = ninit;
+		cont_off[i] = ncont;
+		ninit += (long long)nb * R;
+		ncont += (long long)2 * nb * R;
+		rows_init += nb;
+		rows_cont += 2 * nb;
+		minR = std::min(minR, R);
+	}
+	SolverPools& P = pools;
+	CCF_TRY(P.master_init.ensure(ninit), "cudaMalloc(roots)");
+	CCF_TRY(P.master_cont.ensure(ncont), "cudaMalloc(roots)");
+	CCF_TRY(P.fin_init.ensure(ninit), "cudaMalloc(roots)");
+	CCF_TRY(P.fin_cont.ensure(ncont), "cudaMalloc(roots)");
+	CCF_TRY(P.list_init.ensure(ninit), "cudaMalloc(roots)");
+	CCF_TRY(P.list_cont.ensure(ncont), "cudaMalloc(roots)");
+	if (mixed)
+	{
+		CCF_TRY(P.snap32_init.ensure(ninit), "cudaMalloc(roots)");
+		CCF_TRY(P.snap32_cont.ensure(ncont), "cudaMalloc(roots)");
+	}
+	else
+	{
+		CCF_TRY(P.snap64_init.ensure(ninit), "cudaMalloc(roots)");
+		CCF_TRY(P.snap64_cont.ensure(ncont), "cudaMalloc(roots)");
+	}
+	std::vector<FieldView> views(nf);
+	std::vector<FieldOut> outs(nf);
+	std::vector<const float4*> hilo(nf);
+	std::vector<RowDesc> ri, rc;
+	std::vector<double> cost_i, cost_c;
+	for (int i = 0; i < nf; i++)
+	{
+		Field& f = *fields[i];
+		const int R = f.d.num_roots, N = f.d.num_stars, nb = f.params.num_branches;
+		views[i] = f.view;
+		FieldOut& o = outs[i];
+		std::memset(&o, 0, sizeof(o));
+		o.ccs = f.ccs.ptr;
+		o.caustics = f.params.write_caustics ? f.caustics.ptr : nullptr;
+		o.errs = f.errs.ptr;
+		o.mu = f.params.write_mu_length_scales ? f.mu.ptr : nullptr;
+		o.nb = nb;
+		o.nphi = f.params.num_phi;
+		o.cols = f.params.num_phi / nb + 1;
+		o.half = f.params.num_phi / (2 * nb);
+		o.step_first = 1;
+		o.step_last = o.half;
+		o.max_iters_init = f.params.max_iters_init;
+		o.max_iters_step = f.params.max_iters_step;
+		o.cont_master = P.master_cont.ptr;
+		o.cont_snap32 = mixed ? P.snap32_cont.ptr : nullptr;
+		o.cont_snap64 = mixed ? nullptr : P.snap64_cont.ptr;
+		o.stats = f.stats.ptr;
+		hilo[i] = mixed ? f.star_hilo.ptr : nullptr;
+		double cost = (double)R * (double)(R + N);
+		for (int c = 0; c < nb; c++)
+		{
+			RowDesc r;
+			r.field = i;
+			r.branch = c;
+			r.side = -1;
+			r.pad = 0;
+			r.base = init_off[i] + (long long)c * R;
+			r.cont_base = cont_off[i] + (long long)(2 * c) * R;
+			ri.push_back(r);
+			cost_i.push_back(cost);
+			for (int b = 0; b < 2; b++)
+			{
+				RowDesc q = r;
+				q.side = b;
+				q.base = cont_off[i] + (long long)(2 * c + b) * R;
+				q.cont_base = 0;
+				rc.push_back(q);
+				cost_c.push_back(cost * o.half);
+			}
+		}
+		/* seeds of every branch centre of this field */
+		launch_seed_roots(s, N, R, nb, f.star_gen.ptr, f.view.corner_abs, P.master_init.ptr + init_off[i],
+			mixed ? P.snap32_init.ptr + init_off[i] : nullptr, mixed ? nullptr : P.snap64_init.ptr + init_off[i]);
+	}
+	/* largest rows first */
+	auto order = [](std::vector<RowDesc>& rows, std::vector<double>& cost) {
+		std::vector<int> idx(rows.size());
+		std::iota(idx.begin(), idx.end(), 0);
+		std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+		std::vector<RowDesc> out(rows.size());
+		for (size_t i = 0; i < idx.size(); i++) out[i] = rows[idx[i]];
+		rows.swap(out);
+	};
+	order(ri, cost_i);
+	order(rc, cost_c);
+	CCF_TRY(P.views.ensure(nf), "cudaMalloc(views)");
+	CCF_TRY(P.outs.ensure(nf), "cudaMalloc(outs)");
+	CCF_TRY(P.hilo_ptrs.ensure(nf), "cudaMalloc(views)");
+	CCF_TRY(P.rows_init.ensure(ri.size()), "cudaMalloc(rows)");
+	CCF_TRY(P.rows_cont.ensure(rc.size()), "cudaMalloc(rows)");
+	CCF_TRY(P.error.ensure(1), "cudaMalloc(error)");
+	CCF_TRY(cudaMemcpyAsync(P.views.ptr, views.data(), nf * sizeof(FieldView), cudaMemcpyHostToDevice, s), "upload");
+	CCF_TRY(cudaMemcpyAsync(P.outs.ptr, outs.data(), nf * sizeof(FieldOut), cudaMemcpyHostToDevice, s), "upload");
+	CCF_TRY(cudaMemcpyAsync(P.hilo_ptrs.ptr, hilo.data(), nf * sizeof(const float4*), cudaMemcpyHostToDevice, s), "upload");
+	CCF_TRY(cudaMemcpyAsync(P.rows_init.ptr, ri.data(), ri.size() * sizeof(RowDesc), cudaMemcpyHostToDevice, s), "upload");
+	CCF_TRY(cudaMemcpyAsync(P.rows_cont.ptr, rc.data(), rc.size() * sizeof(RowDesc), cudaMemcpyHostToDevice, s), "upload");
+	CCF_TRY(cudaMemsetAsync(P.error.ptr, 0, sizeof(int), s), "memset");
+
+	/* CTAs per row: fill the resident slots without a second wave */
+	const int slots = num_sms * slots_per_sm;
+	auto pick_cluster = [&](int rows) {
+		int cl = 1;
+		while (cl < 8 && (long long)rows * cl * 2 <= slots && minR / (cl * 2) >= 256) cl *= 2;
+		return cl;
+	};
+	SolveArgs A;
+	std::memset(&A, 0, sizeof(A));
+	A.fields = P.views.ptr;
+	A.outs = P.outs.ptr;
+	A.star_hilo = P.hilo_ptrs.ptr;
+	A.error = P.error.ptr;
+
+	for (Field* f : fields) CCF_TRY(cudaEventRecord(f->ev[3], s), "event");
+	if (verbose >= 1) std::cout << "Finding initial roots...\n";
+	A.rows = P.rows_init.ptr;
+	A.num_rows = (int)ri.size();
+	A.cluster = pick_cluster(A.num_rows);
+	A.master = P.master_init.ptr;
+	A.snap32 = mixed ? P.snap32_init.ptr : nullptr;
+	A.snap64 = mixed ? nullptr : P.snap64_init.ptr;
+	A.fin = P.fin_init.ptr;
+	A.list = P.list_init.ptr;
+	CCF_TRY(launch_solve(s, A, mixed, true), "find_initial_roots");
+	for (Field* f : fields) CCF_TRY(cudaEventRecord(f->ev[4], s), "event");
+	if (verbose >= 1) std::cout << "Finding critical curve positions...\n";
+	A.rows = P.rows_cont.ptr;
+	A.num_rows = (int)rc.size();
+	A.cluster = pick_cluster(A.num_rows);
+	A.master = P.master_cont.ptr;
+	A.snap32 = mixed ? P.snap32_cont.ptr : nullptr;
+	A.snap64 = mixed ? nullptr : P.snap64_cont.ptr;
+	A.fin = P.fin_cont.ptr;
+	A.list = P.list_cont.ptr;
+	CCF_TRY(launch_solve(s, A, mixed, false), "find_ccs");
+	for (Field* f : fields) CCF_TRY(cudaEventRecord(f->ev[5], s), "event");
+	CCF_TRY(cudaStreamSynchronize(s), "solver");
+
+	ccf_status status = CCF_OK;
+	for (Field* f : fields)
+	{
+		unsigned long long st[16];
+		CCF_TRY(cudaMemcpy(st, f->stats.ptr, 16 * sizeof(unsigned long long), cudaMemcpyDeviceToHost), "stats");
+		ccf_info& info = f->info;
+		double me;
+		std::memcpy(&me, &st[0], sizeof(double));
+		info.max_error = me;
+		info.has_nan = st[1] & 1 ? 1 : 0;
+		info.root_updates = (long long)st[2];
+		info.sum_terms = (long long)st[3];
+		info.unconverged = (long long)st[4];
+		info.max_sweeps_init = (int)st[5];
+		info.max_sweeps_step = (int)st[6];
+		info.root_updates_init = (long long)st[7];
+		info.sum_terms_init = (long long)st[8];
+		info.t_stars = ev_ms(f->ev[0], f->ev[1]) * 1e-3;
+		info.t_tree = ev_ms(f->ev[1], f->ev[2]) * 1e-3;
+		info.t_init_roots = ev_ms(f->ev[3], f->ev[4]) * 1e-3;
+		info.t_ccs = ev_ms(f->ev[4], f->ev[5]) * 1e-3;
+		info.t_caustics = 0;
+		info.t_total = ev_ms(f->ev[0], f->ev[5]) * 1e-3;
+		info.kernel_launches += 3;   /* root seeds, initial solve, continuation */
+		if (info.has_nan)
+		{
+			f->error = "Error. Errors in 1/mu contain values which are not positive real numbers.";
+			status = CCF_ERR_NUMERIC;
+		}
+		else
+		{
+			f->ran = true;
+		}
+		if (verbose >= 1)
+		{
+			std::cout << "Done finding critical curve positions. Elapsed time: " << info.t_init_roots + info.t_ccs << " seconds.\n";
+			std::cout << "Maximum error in 1/mu: " << info.max_error << "\n";
+		}
+	}
+	if (status != CCF_OK) error = "Error. Errors in 1/mu contain values which are not positive real numbers.";
+	return status;
+}
+
+ccf_status Engine::run(std::vector<Field*>& fields, int verbose)
+{
+	error.clear();
+	if (fields.empty()) return CCF_OK;
+	if (!ensure_device(fields[0]->params.device)) return CCF_ERR_NO_DEVICE;
+	for (Field* f : fields)
+	{
+		f->ran = false;
+		f->error.clear();
+		ccf_status rc = prepare_field(*f, verbose);
+		if (rc != CCF_OK)
+		{
+			f->error = error;
+			return rc;
+		}
+	}
+	ccf_status rc = solve(fields, verbose);
+	if (rc != CCF_OK)
+	{
+		for (Field* f : fields)
+			if (f->error.empty()) f->error = error;
+	}
+	return rc;
+}
+
+ccf_status Engine::copy_results(Field& f, double* ccs, double* caustics, double* errs, double* mu, double* stars)
+{
+	if (!f.ran) { error = "Error. No results: run() has not completed."; return CCF_ERR_NOT_RUN; }
+	const size_t npts = (size_t)f.d.num_roots * f.params.num_branches * (f.params.num_phi / f.params.num_branches + 1);
+	if (ccs) CCF_TRY(cudaMemcpy(ccs, f.ccs.ptr, npts * sizeof(double2), cudaMemcpyDeviceToHost), "copy ccs");
+	if (errs) CCF_TRY(cudaMemcpy(errs, f.errs.ptr, npts * sizeof(double), cudaMemcpyDeviceToHost), "copy errs");
+	if (caustics)
+	{
+		if (!f.params.write_caustics) { error = "Error. Caustics were not requested (write_caustics = 0)."; return CCF_ERR_INVALID_ARGUMENT; }
+		CCF_TRY(cudaMemcpy(caustics, f.caustics.ptr, npts * sizeof(double2), cudaMemcpyDeviceToHost), "copy caustics");
+	}
+	if (mu)
+	{
+		if (!f.params.write_mu_length_scales) { error = "Error. Length scales were not requested (write_mu_length_scales = 0)."; return CCF_ERR_INVALID_ARGUMENT; }
+		CCF_TRY(cudaMemcpy(mu, f.mu.ptr, npts * sizeof(double), cudaMemcpyDeviceToHost), "copy mu");
+	}
+	if (stars)
+	{
+		const int N = f.d.num_stars;
+		std::vector<double2> pos(N);
+		std::vector<double> mass(N);
+		CCF_TRY(cudaMemcpy(pos.data(), f.star_pos.ptr, N * sizeof(double2), cudaMemcpyDeviceToHost), "copy stars");
+		CCF_TRY(cudaMemcpy(mass.data(), f.star_mass.ptr, N * sizeof(double), cudaMemcpyDeviceToHost), "copy stars");
+		for (int i = 0; i < N; i++)
+		{
+			stars[3 * i] = pos[i].x;
+			stars[3 * i + 1] = pos[i].y;
+			stars[3 * i + 2] = mass[i];
+		}
+	}
+	return CCF_OK;
+}
+
+ccf_status Engine::save(Field& f, int verbose)
+{
+	if (!f.ran) { error = "Error. No results: run() has not completed."; return CCF_ERR_NOT_RUN; }
+	const ccf_params& p = f.params;
+	const std::string prefix = p.outfile_prefix;
+	const bool single = p.output_float != 0;
+	const int R = f.d.num_roots, nb = p.num_branches, cols = p.num_phi / nb + 1;
+	const size_t npts = (size_t)R * nb * cols;
+	if (verbose >= 2) std::cout << "Writing parameter info...\n";
+	std::string fn = prefix + "ccf_parameter_info.txt";
+	if (!write_parameter_info(fn, p, f.info, f.d.star_input))
+	{
+		error = "Error. Failed to open file " + fn;
+		return CCF_ERR_IO;
+	}
+	if (verbose >= 1) std::cout << "Done writing parameter info to file " << fn << "\n";
+	if (p.write_stars)
+	{
+		StarField sf;
+		sf.n = f.d.num_stars;
+		sf.rectangular = f.d.rectangular;
+		sf.corner_x1 = f.d.corner_x1;
+		sf.corner_x2 = f.d.corner_x2;
+		sf.theta = f.d.theta;
+		sf.xym.resize((size_t)3 * sf.n);
+		ccf_status rc = copy_results(f, nullptr, nullptr, nullptr, nullptr, sf.xym.data());
+		if (rc != CCF_OK) return rc;
+		fn = prefix + "ccf_stars.bin";
+		if (!write_star_file(fn, sf, single))
+		{
+			error = "Error. Unable to write star info to file " + fn;
+			return CCF_ERR_IO;
+		}
+		if (verbose >= 1) std::cout << "Done writing star info to file " << fn << "\n";
+	}
+	std::vector<double> buf;
+	if (p.write_critical_curves)
+	{
+		buf.resize(2 * npts);
+		ccf_status rc = copy_results(f, buf.data(), nullptr, nullptr, nullptr, nullptr);
+		if (rc != CCF_OK) return rc;
+		fn = prefix + "ccf_ccs.bin";
+		if (!write_array_complex(fn, buf.data(), R * nb, cols, single))
+		{
+			error = "Error. Unable to write ccs info to file " + fn;
+			return CCF_ERR_IO;
+		}
+		if (verbose >= 1) std::cout << "Done writing critical curve positions to file " << fn << "\n";
+	}
+	if (p.write_caustics)
+	{
+		buf.resize(2 * npts);
+		ccf_status rc = copy_results(f, nullptr, buf.data(), nullptr, nullptr, nullptr);
+		if (rc != CCF_OK) return rc;
+		fn = prefix + "ccf_caustics.bin";
+		if (!write_array_complex(fn, buf.data(), R * nb, cols, single))
+		{
+			error = "Error. Unable to write caustic info to file " + fn;
+			return CCF_ERR_IO;
+		}
+		if (verbose >= 1) std::cout << "Done writing caustic positions to file " << fn << "\n";
+	}
+	if (p.write_mu_length_scales)
+	{
+		buf.resize(npts);
+		ccf_status rc = copy_results(f, nullptr, nullptr, nullptr, buf.data(), nullptr);
+		if (rc != CCF_OK) return rc;
+		fn = prefix + "ccf_mu_length_scales.bin";
+		if (!write_array_real(fn, buf.data(), R * nb, cols, single))
+		{
+			error = "Error. Unable to write magnification length scales info to file " + fn;
+			return CCF_ERR_IO;
+		}
+		if (verbose >= 1) std::cout << "Done writing magnification length scales to file " << fn << "\n";
+	}
+	return CCF_OK;
+}
+
+} /* namespace ccf */

@@ -1,0 +1,174 @@
+/******************************************************************************
+engine.h -- host orchestration of one star field on the device (the role of
+CCF<T>::run / save, include/ccf.cuh:1265-1287) and of batches of fields.
+******************************************************************************/
+#pragma once
+
+#include "kernels.h"
+#include "params.h"
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace ccf
+{
+
+/* grow-only device buffer: repeated runs of one configuration allocate once */
+template <typename T>
+struct DBuf
+{
+	T* ptr = nullptr;
+	size_t cap = 0;
+	size_t n = 0;
+	DBuf() = default;
+	DBuf(const DBuf&) = delete;
+	DBuf& operator=(const DBuf&) = delete;
+	~DBuf() { release(); }
+	void release()
+	{
+		if (ptr) cudaFree(ptr);
+		ptr = nullptr;
+		cap = 0;
+		n = 0;
+	}
+	cudaError_t ensure(size_t count)
+	{
+		n = count;
+		if (count <= cap && ptr) return cudaSuccess;
+		if (ptr) cudaFree(ptr);
+		ptr = nullptr;
+		cap = 0;
+		size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+		cudaError_t e = cudaMalloc((void**)&ptr, bytes);
+		if (e == cudaSuccess) cap = std::max<size_t>(count, 1);
+		return e;
+	}
+	/* grow keeping the first `keep` elements */
+	cudaError_t grow(size_t count, size_t keep, cudaStream_t s)
+	{
+		if (count <= cap && ptr) { n = count; return cudaSuccess; }
+		T* np = nullptr;
+		cudaError_t e = cudaMalloc((void**)&np, count * sizeof(T));
+		if (e != cudaSuccess) return e;
+		if (ptr && keep) cudaMemcpyAsync(np, ptr, keep * sizeof(T), cudaMemcpyDeviceToDevice, s);
+		cudaStreamSynchronize(s);
+		if (ptr) cudaFree(ptr);
+		ptr = np;
+		cap = count;
+		n = count;
+		return cudaSuccess;
+	}
+	size_t bytes() const { return cap * sizeof(T); }
+};
+
+/* one field: parameters, derived values, device-resident star field, tree,
+   FMM, leaf records and outputs */
+struct Field
+{
+	ccf_params params;
+	ccf_info info;
+	Derived d;
+	std::unique_ptr<StarField> user_stars;   /* set by ccf_set_stars */
+	bool ran = false;
+	std::string error;
+
+	/* stars: generation order (seeds) and tree order */
+	DBuf<double2> star_gen;
+	DBuf<double2> star_pos, star_tmp_pos;
+	DBuf<double> star_mass, star_tmp_mass;
+	DBuf<float4> star_hilo;
+	DBuf<double> stats5;
+
+	/* tree */
+	DBuf<double2> n_center;
+	DBuf<double> n_half;
+	DBuf<int> n_level, n_parent, n_child, n_sstart, n_scount, n_nbr, n_nbrc, n_m2l, n_m2lc, n_p2l, n_p2lc, n_flag, n_rank;
+	DBuf<int> level_out;   /* [max, nflag, err] */
+	int node_cap = 0;
+	int num_nodes = 0;
+	std::vector<int> level_start, level_count;
+
+	/* FMM and leaves */
+	DBuf<double> binom;
+	DBuf<double2> multi, local;
+	DBuf<int> leaf_flag, leaf_index, node_leaf;
+	DBuf<double2> leaf_center;
+	DBuf<double> leaf_inv_half;
+	DBuf<int> leaf_near_count;
+	DBuf<NearStar> leaf_near;
+	DBuf<double2> leaf_loc;
+	DBuf<float2> leaf_loc3f;
+	int num_leaves = 0;
+
+	/* smooth-mass polynomials */
+	DBuf<double2> sm_d1, sm_d2, sm_a;
+	DBuf<float2> sm_d2f;
+
+	/* device view */
+	FieldView view;
+	DBuf<FieldView> view_dev;
+
+	/* outputs, file layout */
+	DBuf<double2> ccs, caustics;
+	DBuf<double> errs, mu;
+	DBuf<unsigned long long> stats;   /* solver statistics, 8 words */
+
+	/* timing */
+	cudaEvent_t ev[8] = {};
+	bool events = false;
+
+	~Field();
+	TreeDev tree_dev() const;
+};
+
+/* solver row pools shared by the fields of a batch */
+struct SolverPools
+{
+	DBuf<double2> master_init, master_cont, snap64_init, snap64_cont;
+	DBuf<float4> snap32_init, snap32_cont;
+	DBuf<unsigned char> fin_init, fin_cont;
+	DBuf<int> list_init, list_cont;
+	DBuf<RowDesc> rows_init, rows_cont;
+	DBuf<FieldView> views;
+	DBuf<FieldOut> outs;
+	DBuf<const float4*> hilo_ptrs;
+	DBuf<int> error;
+};
+
+class Engine
+{
+public:
+	Engine();
+	~Engine();
+
+	/* run a batch of fields (size 1 for ccf_run) */
+	ccf_status run(std::vector<Field*>& fields, int verbose);
+	ccf_status save(Field& f, int verbose);
+	ccf_status copy_results(Field& f, double* ccs, double* caustics, double* errs, double* mu, double* stars);
+
+	cudaStream_t stream = nullptr;
+	int device = 0;
+	int num_sms = 0;
+	std::string error;
+
+private:
+	ccf_status prepare_field(Field& f, int verbose);
+	ccf_status build_tree(Field& f);
+	ccf_status build_fmm(Field& f);
+	ccf_status solve(std::vector<Field*>& fields, int verbose);
+	ccf_status cuda_fail(cudaError_t e, const char* what);
+
+public:
+	bool ensure_device(int dev);
+
+private:
+
+	SolverPools pools;
+	bool initialized = false;
+	int slots_per_sm = 1;
+};
+
+} /* namespace ccf */

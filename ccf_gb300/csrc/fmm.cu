@@ -1,0 +1,281 @@
+/******************************************************************************
+fmm.cu -- 2-D complex fast multipole passes on the device, FP64.
+
+Expansions of the log potential sum m_i log(z - z_i), in units of the node
+half-length, as in the reference (include/fmm.cuh): multipole coefficients
+a_0 = sum m, a_k = -sum m ((z_i - c)/h)^k / k; local coefficients c_l of
+sum c_l ((z - c)/h)^l.  Translations:
+  P2M  fmm.cuh:21-49       M2M  fmm.cuh:109-139      L2L  fmm.cuh:204-223
+  M2L  fmm.cuh:281-322     P2L  fmm.cuh:387-413
+Layout: one warp per node, lane p computes coefficient p (order <= 31, so a
+whole expansion is one warp).  Each translation is written as a Horner
+recurrence with a single complex reciprocal, instead of the reference's
+division per term.  The binomial table is passed in: by default it holds the
+reference's int32 Pascal triangle (whose entries above n = 33 wrap), because
+the reference's M2L uses those values and its roots depend on them.
+******************************************************************************/
+#include "kernels.h"
+
+namespace ccf
+{
+
+CCF_D double binom_at(const double* __restrict__ B, int n, int k)
+{
+	if (n < k) return 0;
+	return B[n * (n + 1) / 2 + k];
+}
+
+CCF_D double2 cpow_int(double2 a, int p)
+{
+	double2 r = make_double2(1, 0);
+	for (int i = 0; i < p; i++) r = cmul(r, a);
+	return r;
+}
+
+/* upward pass at one level: P2M for leaves holding stars, M2M for split nodes */
+__global__ void fmm_upward_kernel(TreeDev T, int start, int count, int P, const double2* __restrict__ pos,
+	const double* __restrict__ mass, double2* __restrict__ multi, const double* __restrict__ B)
+{
+	int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	int p = threadIdx.x & 31;
+	if (w >= count) return;
+	int n = start + w;
+	if (p > P) return;
+	double2 r = make_double2(0, 0);
+	int ch = T.child[n];
+	if (ch < 0)
+	{
+		int s = T.star_start[n], ns = T.star_count[n];
+		if (ns == 0) return;
+		double2 c = T.center[n];
+		double ih = 1.0 / T.half[n];
+		for (int i = 0; i < ns; i++)
+		{
+			double m = mass[s + i];
+			if (p == 0)
+			{
+				r.x += m;
+			}
+			else
+			{
+				double2 q = pos[s + i];
+				double2 wz = make_double2((q.x - c.x) * ih, (q.y - c.y) * ih);
+				double2 t = cpow_int(wz, p);
+				r.x -= t.x * m;
+				r.y -= t.y * m;
+			}
+		}
+		if (p > 0)
+		{
+			r.x /= p;
+			r.y /= p;
+		}
+	}
+	else
+	{
+		double2 pc = T.center[n];
+		for (int q = 0; q < 4; q++)
+		{
+			int k = ch + q;
+			const double2* a = multi + (size_t)k * (P + 1);
+			double2 v;
+			if (p == 0)
+			{
+				v = a[0];
+			}
+			else
+			{
+				double2 cc = T.center[k];
+				double ih = 1.0 / T.half[k];
+				double2 dz = make_double2((cc.x - pc.x) * ih, (cc.y - pc.y) * ih);
+				/* b_p = (sum_{i=1..p} a_i C(p-1, i-1) dz^(p-i) - a_0 dz^p / p) / 2^p */
+				double2 acc = cscale(a[1], binom_at(B, p - 1, 0));
+				for (int i = 2; i <= p; i++) acc = cadd(cmul(acc, dz), cscale(a[i], binom_at(B, p - 1, i - 1)));
+				double2 dzp = cpow_int(dz, p);
+				double2 t = cscale(cmul(a[0], dzp), 1.0 / p);
+				v = cscale(csub(acc, t), ldexp(1.0, -p));
+			}
+			r = cadd(r, v);
+		}
+	}
+	multi[(size_t)n * (P + 1) + p] = r;
+}
+
+/* downward pass at one level >= 2: L2L from the parent, then M2L from the
+   same-level interaction list, then P2L from the coarser-leaf list, summed
+   in that order (include/ccf.cuh:880-893) */
+__global__ void fmm_downward_kernel(TreeDev T, int start, int count, int P, const double2* __restrict__ pos,
+	const double* __restrict__ mass, const double2* __restrict__ multi, double2* __restrict__ local,
+	const double* __restrict__ B)
+{
+	int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	int p = threadIdx.x & 31;
+	if (w >= count) return;
+	int n = start + w;
+	if (p > P) return;
+	double2 cn = T.center[n];
+	double2 r = make_double2(0, 0);
+	/* L2L: d_p = sum_{k>=max(p,1)} c_k C(k,p) dz^(k-p) / 2^p, dz = (c - c_parent)/h_parent */
+	{
+		int par = T.parent[n];
+		const double2* cl = local + (size_t)par * (P + 1);
+		double2 pcn = T.center[par];
+		double ih = 1.0 / T.half[par];
+		double2 dz = make_double2((cn.x - pcn.x) * ih, (cn.y - pcn.y) * ih);
+		int k0 = p > 1 ? p : 1;
+		double2 acc = cscale(cl[P], binom_at(B, P, p));
+		for (int k = P - 1; k >= k0; k--) acc = cadd(cmul(acc, dz), cscale(cl[k], binom_at(B, k, p)));
+		if (p == 0) acc = cmul(acc, dz);
+		r = cscale(acc, ldexp(1.0, -p));
+	}
+	/* M2L: t = 1/(-dz), dz = (c_from - c_to)/h_from;
+	   c_0 = sum_k b_k t^k + b_0 log(-dz) + b_0 log h_from
+	   c_p = (sum_k b_k C(p+k-1, k-1) t^k - b_0/p) (-t)^p */
+	int nm = T.m2l_count[n];
+	for (int j = 0; j < nm; j++)
+	{
+		int f = T.m2l[n * MAX_M2L + j];
+		const double2* b = multi + (size_t)f * (P + 1);
+		double2 cf = T.center[f];
+		double hf = T.half[f];
+		double ih = 1.0 / hf;
+		double2 dz = make_double2((cf.x - cn.x) * ih, (cf.y - cn.y) * ih);
+		double2 t = cinv(make_double2(-dz.x, -dz.y));
+		double2 acc = cscale(b[P], binom_at(B, p + P - 1, P - 1));
+		for (int k = P - 1; k >= 1; k--) acc = cadd(cmul(acc, t), cscale(b[k], binom_at(B, p + k - 1, k - 1)));
+		acc = cmul(acc, t);
+		double2 v;
+		if (p == 0)
+		{
+			double2 lg = make_double2(log(hypot(dz.x, dz.y)), atan2(-dz.y, -dz.x));
+			v = cadd(cadd(acc, cmul(b[0], lg)), cscale(b[0], log(hf)));
+		}
+		else
+		{
+			double2 mt = make_double2(-t.x, -t.y);
+			v = cmul(csub(acc, cscale(b[0], 1.0 / p)), cpow_int(mt, p));
+		}
+		r = cadd(r, v);
+	}
+	/* P2L: c_0 = sum m log(-w) + m log h, c_p = -sum m / (p w^p), w = (z_i - c)/h */
+	int np = T.p2l_count[n];
+	double hn = T.half[n];
+	double ihn = 1.0 / hn;
+	double lhn = log(hn);
+	for (int j = 0; j < np; j++)
+	{
+		int f = T.p2l[n * MAX_P2L + j];
+		int s = T.star_start[f], ns = T.star_count[f];
+		double2 v = make_double2(0, 0);
+		for (int i = 0; i < ns; i++)
+		{
+			double2 q = pos[s + i];
+			double m = mass[s + i];
+			double2 wz = make_double2((q.x - cn.x) * ihn, (q.y - cn.y) * ihn);
+			if (p == 0)
+			{
+				double2 lg = make_double2(log(hypot(wz.x, wz.y)), atan2(-wz.y, -wz.x));
+				v.x += m * lg.x + m * lhn;
+				v.y += m * lg.y;
+			}
+			else
+			{
+				double2 iw = cinv(wz);
+				double2 t = cpow_int(iw, p);
+				v.x -= m * t.x / p;
+				v.y -= m * t.y / p;
+			}
+		}
+		r = cadd(r, v);
+	}
+	local[(size_t)n * (P + 1) + p] = r;
+}
+
+/* leaf records for the solver: centre, 1/h, packed near stars (neighbours
+   first, then the leaf's own stars, as include/alpha_star.cuh:26-37 sums
+   them) and the local coefficients pre-scaled for alpha, d/dzbar, d2/dzbar2:
+   L1_i = theta^2 i c_i / h, L2_i = theta^2 i (i-1) c_i / h^2,
+   L3_i = theta^2 i (i-1) (i-2) c_i / h^3 */
+__global__ void leaf_build_kernel(TreeDev T, int num_nodes, const int* __restrict__ leaf_index, int P, double theta2,
+	const double2* __restrict__ pos, const double* __restrict__ mass, const double2* __restrict__ local,
+	double2* __restrict__ leaf_center, double* __restrict__ leaf_inv_half, int* __restrict__ leaf_near_count,
+	NearStar* __restrict__ leaf_near, double2* __restrict__ leaf_loc, float2* __restrict__ leaf_loc3f,
+	int* __restrict__ node_leaf, int* err)
+{
+	int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	int lane = threadIdx.x & 31;
+	if (w >= num_nodes) return;
+	int n = w;
+	if (T.child[n] >= 0) return;
+	int l = leaf_index[n];
+	if (lane == 0)
+	{
+		node_leaf[n] = l;
+		leaf_center[l] = T.center[n];
+		leaf_inv_half[l] = 1.0 / T.half[n];
+	}
+	/* near list */
+	if (lane == 0)
+	{
+		int cnt = 0;
+		NearStar* out = leaf_near + (size_t)l * MAX_NEAR;
+		int k = T.nbr_count[n];
+		for (int j = 0; j <= k; j++)
+		{
+			int src = j < k ? T.nbr[n * MAX_NBR + j] : n;
+			int s = T.star_start[src], ns = T.star_count[src];
+			for (int i = 0; i < ns; i++)
+			{
+				if (cnt < MAX_NEAR)
+				{
+					double2 q = pos[s + i];
+					out[cnt].x = q.x;
+					out[cnt].y = q.y;
+					out[cnt].m = mass[s + i];
+					out[cnt].pad = 0;
+				}
+				cnt++;
+			}
+		}
+		if (cnt > MAX_NEAR) atomicOr(err, 2);
+		leaf_near_count[l] = cnt < MAX_NEAR ? cnt : MAX_NEAR;
+	}
+	/* scaled local coefficients */
+	for (int i = lane; i <= P; i += 32)
+	{
+		double2 c = local[(size_t)n * (P + 1) + i];
+		double ih = 1.0 / T.half[n];
+		double f1 = theta2 * i * ih;
+		double f2 = theta2 * i * (i - 1) * ih * ih;
+		double f3 = theta2 * i * (i - 1) * (i - 2) * ih * ih * ih;
+		double2* L = leaf_loc + (size_t)l * 3 * (P + 1);
+		L[i] = cscale(c, f1);
+		L[(P + 1) + i] = cscale(c, f2);
+		double2 c3 = cscale(c, f3);
+		L[2 * (P + 1) + i] = c3;
+		leaf_loc3f[(size_t)l * (P + 1) + i] = make_float2((float)c3.x, (float)c3.y);
+	}
+}
+
+void launch_fmm_upward(cudaStream_t s, const TreeDev& T, int start, int count, int P, const double2* pos, const double* mass,
+	double2* multi, const double* B)
+{
+	long long threads = (long long)count * 32;
+	fmm_upward_kernel<<<(int)((threads + 127) / 128), 128, 0, s>>>(T, start, count, P, pos, mass, multi, B);
+}
+void launch_fmm_downward(cudaStream_t s, const TreeDev& T, int start, int count, int P, const double2* pos, const double* mass,
+	const double2* multi, double2* local, const double* B)
+{
+	long long threads = (long long)count * 32;
+	fmm_downward_kernel<<<(int)((threads + 127) / 128), 128, 0, s>>>(T, start, count, P, pos, mass, multi, local, B);
+}
+void launch_leaf_build(cudaStream_t s, const TreeDev& T, int num_nodes, const int* leaf_index, int P, double theta2,
+	const double2* pos, const double* mass, const double2* local, double2* leaf_center, double* leaf_inv_half,
+	int* leaf_near_count, NearStar* leaf_near, double2* leaf_loc, float2* leaf_loc3f, int* node_leaf, int* err)
+{
+	long long threads = (long long)num_nodes * 32;
+	leaf_build_kernel<<<(int)((threads + 127) / 128), 128, 0, s>>>(T, num_nodes, leaf_index, P, theta2, pos, mass, local,
+		leaf_center, leaf_inv_half, leaf_near_count, leaf_near, leaf_loc, leaf_loc3f, node_leaf, err);
+}
+
+} /* namespace ccf */

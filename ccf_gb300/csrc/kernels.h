@@ -1,0 +1,126 @@
+/******************************************************************************
+kernels.h -- device data structures shared by the kernels and the host
+engine, and the host-side launch functions of every kernel.
+******************************************************************************/
+#pragma once
+
+#include "common.cuh"
+#include "field.cuh"
+#include "mass.h"
+
+#include <algorithm>
+
+namespace ccf
+{
+
+constexpr int MAX_NBR = 8;    /* include/tree_node.cuh:23 */
+constexpr int MAX_M2L = 27;   /* include/tree_node.cuh:24 */
+constexpr int MAX_P2L = 5;    /* include/tree_node.cuh:25 */
+
+/* quadtree nodes, structure of arrays; nodes of a level are contiguous */
+struct TreeDev
+{
+	double2* center;
+	double* half;
+	int* level;
+	int* parent;
+	int* child;        /* first of four contiguous children, -1 for a leaf */
+	int* star_start;
+	int* star_count;
+	int* nbr;          /* [node * MAX_NBR + j] */
+	int* nbr_count;
+	int* m2l;          /* [node * MAX_M2L + j] */
+	int* m2l_count;
+	int* p2l;          /* [node * MAX_P2L + j] */
+	int* p2l_count;
+	int* flag;         /* split flag of the level being built */
+	int* rank;         /* exclusive scan of flag */
+};
+
+/* one row of the root solver: all roots of one branch centre (initial
+   solve) or of one (branch, side) continuation */
+struct RowDesc
+{
+	int field;         /* index into the launch's FieldView / FieldOut arrays */
+	int branch;        /* c */
+	int side;          /* -1: initial solve at the branch centre; 0: phi decreasing; 1: increasing */
+	int pad;
+	long long base;    /* offset of the row in master / snapshot / fin / list */
+	long long cont_base; /* initial rows: offset of the (branch, side 0) continuation row */
+};
+
+/* per-field outputs and statistics of a solver launch */
+struct FieldOut
+{
+	double2* ccs;          /* file layout, rows = R * nb, cols */
+	double2* caustics;     /* may be null */
+	double* errs;
+	double* mu;            /* may be null */
+	int nb;
+	int nphi;
+	int cols;
+	int half;              /* nphi / (2 nb) */
+	int step_first;        /* continuation steps to run: [step_first, step_last] */
+	int step_last;
+	int max_iters_init;
+	int max_iters_step;
+	/* continuation arrays that the initial solve fills for both sides */
+	double2* cont_master;
+	float4* cont_snap32;
+	double2* cont_snap64;
+	/* statistics */
+	unsigned long long* stats;   /* [0] max_err bits, [1] nan flag, [2] updates, [3] terms,
+	                                [4] unconverged, [5] max sweeps init, [6] max sweeps step,
+	                                [7] updates in the initial solve, [8] terms in the initial solve */
+};
+
+struct SolveArgs
+{
+	const FieldView* fields;
+	const FieldOut* outs;
+	const RowDesc* rows;
+	int num_rows;
+	int cluster;           /* CTAs per row */
+	double2* master;
+	float4* snap32;
+	double2* snap64;
+	unsigned char* fin;
+	int* list;
+	const float4* const* star_hilo;   /* per field, FP32 hi/lo stars (mixed) */
+	int* error;
+};
+
+/* stars.cu */
+void launch_generate_stars(cudaStream_t s, int n, int seed, int rectangular, double2 corner, double corner_abs,
+	const MassTable& mt, double2* pos, double* mass);
+void launch_star_stats(cudaStream_t s, int n, const double* mass, double* out);
+void launch_seed_roots(cudaStream_t s, int nstars, int nroots, int nrows, const double2* pos, double corner_abs,
+	double2* master, float4* snap32, double2* snap64);
+void launch_star_hilo(cudaStream_t s, int n, const double2* pos, float4* out);
+
+/* tree.cu */
+void launch_tree_root(cudaStream_t s, const TreeDev& T, double half, int nstars);
+void launch_tree_flag(cudaStream_t s, const TreeDev& T, int start, int count, int* out);
+void launch_scan(cudaStream_t s, const int* in, int* out, int n);
+void launch_tree_children(cudaStream_t s, const TreeDev& T, int start, int count, int child_start);
+void launch_tree_partition(cudaStream_t s, const TreeDev& T, int start, int count, double2* pos, double* mass,
+	double2* tpos, double* tmass);
+void launch_tree_neighbors(cudaStream_t s, const TreeDev& T, int start, int count, int* err);
+void launch_leaf_flag(cudaStream_t s, const TreeDev& T, int num_nodes, int* flag);
+
+/* fmm.cu */
+void launch_fmm_upward(cudaStream_t s, const TreeDev& T, int start, int count, int P, const double2* pos, const double* mass,
+	double2* multi, const double* B);
+void launch_fmm_downward(cudaStream_t s, const TreeDev& T, int start, int count, int P, const double2* pos, const double* mass,
+	const double2* multi, double2* local, const double* B);
+void launch_leaf_build(cudaStream_t s, const TreeDev& T, int num_nodes, const int* leaf_index, int P, double theta2,
+	const double2* pos, const double* mass, const double2* local, double2* leaf_center, double* leaf_inv_half,
+	int* leaf_near_count, NearStar* leaf_near, double2* leaf_loc, float2* leaf_loc3f, int* node_leaf, int* err);
+
+/* solver.cu */
+int solver_blocks_per_sm(bool mixed);
+cudaError_t launch_solve(cudaStream_t s, const SolveArgs& a, bool mixed, bool initial);
+cudaError_t launch_eval_points(cudaStream_t s, const FieldView* F_dev, int npts, const double2* z, const double* phi,
+	double2* f, double2* df, double2* w, double* err, double* mu);
+
+} /* namespace ccf */

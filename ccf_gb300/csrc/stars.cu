@@ -1,0 +1,145 @@
+/******************************************************************************
+stars.cu -- seeded star-field generation, star statistics and root seeds.
+
+Random numbers: curand's XORWOW generator, one subsequence per star
+(curand_init(seed, i, 0)), three uniform doubles per star in the order
+(x1 or angle, x2 or radius, mass) -- the stream the reference draws
+(include/star.cuh:40-107), so a seed gives the reference's star field.
+The state lives in registers for the one thread that draws the star; nothing
+is written back.
+******************************************************************************/
+#include "kernels.h"
+
+#include <curand_kernel.h>
+
+namespace ccf
+{
+
+__global__ void __launch_bounds__(256) generate_stars_kernel(int n, int seed, int rectangular, double2 corner, double corner_abs,
+	MassTable mt, double2* __restrict__ pos, double* __restrict__ mass)
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	curandStateXORWOW_t st;
+	curand_init(seed, i, 0, &st);
+	double x1, x2;
+	if (rectangular)
+	{
+		x1 = curand_uniform_double(&st) * 2 * corner.x - corner.x;
+		x2 = curand_uniform_double(&st) * 2 * corner.y - corner.y;
+	}
+	else
+	{
+		double a = curand_uniform_double(&st) * 2 * PI;
+		double r = sqrt(curand_uniform_double(&st)) * corner_abs;
+		double s, c;
+		sincos(a, &s, &c);
+		x1 = r * c;
+		x2 = r * s;
+	}
+	pos[i] = make_double2(x1, x2);
+	mass[i] = mass_draw(mt, curand_uniform_double(&st));
+}
+
+/* Deterministic single-block reduction of the star statistics of
+   include/star.cuh:124-161: total mass, sum m^2, sum m^2 ln m, min, max. */
+__global__ void __launch_bounds__(1024) star_stats_kernel(int n, const double* __restrict__ mass, double* out)
+{
+	__shared__ double s_m[1024], s_m2[1024], s_l[1024], s_lo[1024], s_hi[1024];
+	double m1 = 0, m2 = 0, ml = 0, lo = 1.7976931348623157e308, hi = 2.2250738585072014e-308;
+	for (int i = threadIdx.x; i < n; i += blockDim.x)
+	{
+		double m = mass[i];
+		m1 += m;
+		m2 += m * m;
+		ml += m * m * log(m);
+		lo = fmin(lo, m);
+		hi = fmax(hi, m);
+	}
+	s_m[threadIdx.x] = m1;
+	s_m2[threadIdx.x] = m2;
+	s_l[threadIdx.x] = ml;
+	s_lo[threadIdx.x] = lo;
+	s_hi[threadIdx.x] = hi;
+	__syncthreads();
+	for (int s = blockDim.x / 2; s > 0; s >>= 1)
+	{
+		if (threadIdx.x < s)
+		{
+			s_m[threadIdx.x] += s_m[threadIdx.x + s];
+			s_m2[threadIdx.x] += s_m2[threadIdx.x + s];
+			s_l[threadIdx.x] += s_l[threadIdx.x + s];
+			s_lo[threadIdx.x] = fmin(s_lo[threadIdx.x], s_lo[threadIdx.x + s]);
+			s_hi[threadIdx.x] = fmax(s_hi[threadIdx.x], s_hi[threadIdx.x + s]);
+		}
+		__syncthreads();
+	}
+	if (threadIdx.x == 0)
+	{
+		out[0] = s_m[0];
+		out[1] = s_m2[0];
+		out[2] = s_l[0];
+		out[3] = s_lo[0];
+		out[4] = s_hi[0];
+	}
+}
+
+/* Initial roots of a branch centre (include/ccf.cuh:711-726): z_i + 1 and
+   z_i - 1 for every star in generation order, then the extra roots of the
+   rectangular Taylor form evenly on the circle of radius |corner|.
+   Writes rows [row0, row0 + nrows) of master / snapshot. */
+__global__ void seed_roots_kernel(int nstars, int nroots, int nrows, const double2* __restrict__ pos, double corner_abs,
+	double2* __restrict__ master, float4* __restrict__ snap32, double2* __restrict__ snap64)
+{
+	long long total = (long long)nrows * nroots;
+	int extra = nroots - 2 * nstars;
+	for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x)
+	{
+		int a = (int)(q % nroots);
+		double2 z;
+		if (a < nstars) z = make_double2(pos[a].x + 1, pos[a].y);
+		else if (a < 2 * nstars) z = make_double2(pos[a - nstars].x - 1, pos[a - nstars].y);
+		else
+		{
+			int i = a - 2 * nstars;
+			double t = 2 * PI / extra * i;
+			z = make_double2(corner_abs * cos(t), corner_abs * sin(t));
+		}
+		master[q] = z;
+		if (snap32) snap32[q] = split_hilo(z);
+		if (snap64) snap64[q] = z;
+	}
+}
+
+/* FP32 hi/lo form of the star positions, the poles of the Aberth sums */
+__global__ void star_hilo_kernel(int n, const double2* __restrict__ pos, float4* __restrict__ out)
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < n) out[i] = split_hilo(pos[i]);
+}
+
+void launch_generate_stars(cudaStream_t s, int n, int seed, int rectangular, double2 corner, double corner_abs,
+	const MassTable& mt, double2* pos, double* mass)
+{
+	generate_stars_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, seed, rectangular, corner, corner_abs, mt, pos, mass);
+}
+
+void launch_star_stats(cudaStream_t s, int n, const double* mass, double* out)
+{
+	star_stats_kernel<<<1, 1024, 0, s>>>(n, mass, out);
+}
+
+void launch_seed_roots(cudaStream_t s, int nstars, int nroots, int nrows, const double2* pos, double corner_abs,
+	double2* master, float4* snap32, double2* snap64)
+{
+	long long total = (long long)nrows * nroots;
+	int blocks = (int)std::min<long long>((total + 255) / 256, 152 * 16);
+	seed_roots_kernel<<<blocks, 256, 0, s>>>(nstars, nroots, nrows, pos, corner_abs, master, snap32, snap64);
+}
+
+void launch_star_hilo(cudaStream_t s, int n, const double2* pos, float4* out)
+{
+	star_hilo_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, pos, out);
+}
+
+} /* namespace ccf */

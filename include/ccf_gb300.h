@@ -1,0 +1,225 @@
+/******************************************************************************
+ccf_gb300.h -- C ABI of the GB300-native critical-curve and caustic finder.
+
+The reference (weisluke/ccf) exports no extern "C" surface: its operator API
+is the header-only class template CCF<T> (include/ccf.cuh:34-1289) and the
+main_ccf command line (src/main_ccf.cu).  Every entry point below states the
+reference interface it replaces.  Signatures use plain C types and pointers
+only, so that C, C++, Python ctypes/cffi or any other FFI can bind them.
+
+Thread safety: one handle must not be used from two threads at once;
+different handles are independent.  All work runs on CUDA device 0 (the
+reference's choice, include/ccf.cuh:205-212) unless ccf_params.device says
+otherwise.  The library never resets the CUDA context (the reference calls
+cudaDeviceReset on every run, include/ccf.cuh:151, which a long-lived caller
+cannot afford).
+******************************************************************************/
+#ifndef CCF_GB300_H
+#define CCF_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CCF_GB300_ABI_VERSION 1
+
+/* Status codes.  The reference returns bool from every stage and prints the
+   reason to std::cerr (include/ccf.cuh:1265-1287); here the reason is kept
+   per handle and returned by ccf_last_error(). */
+typedef enum ccf_status
+{
+	CCF_OK = 0,
+	CCF_ERR_INVALID_ARGUMENT = 1, /* input check failed (include/ccf.cuh:218-346) */
+	CCF_ERR_CUDA = 2,             /* a CUDA call failed (include/util.cuh:156-190) */
+	CCF_ERR_NO_DEVICE = 3,        /* no CUDA device (include/ccf.cuh:185-189) */
+	CCF_ERR_OUT_OF_MEMORY = 4,
+	CCF_ERR_IO = 5,               /* star file or output file problem */
+	CCF_ERR_NOT_RUN = 6,          /* results asked for before a successful run */
+	CCF_ERR_NUMERIC = 7,          /* non-finite 1/mu errors (include/ccf.cuh:963-967) */
+	CCF_ERR_TIMEOUT = 8,          /* a bounded device-side wait ran out */
+	CCF_ERR_BUDGET = 9            /* request larger than the device-memory budget */
+} ccf_status;
+
+/* Arithmetic used by the root solver. */
+typedef enum ccf_precision
+{
+	CCF_PRECISION_FP64 = 0,  /* all solver arithmetic in FP64 */
+	CCF_PRECISION_MIXED = 1  /* FP32 Aberth correction sums, FP64 critical-curve
+	                            function, residual and caustic map */
+} ccf_precision;
+
+/* Parameters.  The first block mirrors the public fields of CCF<T> with the
+   same names, meanings and defaults (include/ccf.cuh:42-62); the second block
+   is specific to this implementation.  Fill with ccf_default_params(). */
+typedef struct ccf_params
+{
+	double kappa_tot;            /* default 0.3  */
+	double shear;                /* default 0.3  */
+	double kappa_star;           /* default 0.27 */
+	double theta_star;           /* default 1    */
+	char mass_function[32];      /* "equal", "uniform", "salpeter", "kroupa", "optical_depth" */
+	double m_solar;              /* default 1    */
+	double m_lower;              /* default 0.01 */
+	double m_upper;              /* default 50   */
+	int rectangular;             /* default 0    */
+	int approx;                  /* default 1    */
+	double safety_scale;         /* default 1.37 */
+	int num_stars;               /* default 137  */
+	char starfile[1024];         /* default ""   */
+	int num_phi;                 /* default 100  */
+	int num_branches;            /* default 1    */
+	int random_seed;             /* default 0 (= draw from the clock) */
+	int write_stars;             /* default 1    */
+	int write_critical_curves;   /* default 1    */
+	int write_caustics;          /* default 1    */
+	int write_mu_length_scales;  /* default 0    */
+	char outfile_prefix[1024];   /* default "./" */
+
+	int precision;               /* ccf_precision, default CCF_PRECISION_MIXED */
+	int output_float;            /* 1: write files in single precision, as the
+	                                reference built with -D is_float does */
+	int max_iters_init;          /* cap on Aberth sweeps at a branch centre (default 300) */
+	int max_iters_step;          /* cap on Aberth sweeps per phi step (default 60) */
+	int exact_binomials;         /* 1: exact binomials in the FMM translations;
+	                                0 (default): the reference's int32 table */
+	int device;                  /* CUDA device ordinal, default 0 */
+	int reserved[8];
+} ccf_params;
+
+/* Derived parameters, statistics and timings of a run.  Names follow the keys
+   of ccf_parameter_info.txt (include/ccf.cuh:1142-1191). */
+typedef struct ccf_info
+{
+	int num_stars;
+	int num_roots;
+	int taylor_smooth;
+	int tree_levels;
+	int expansion_order;
+	int num_nodes;
+	int num_leaves;
+	int rectangular;
+	int random_seed;
+	int has_nan;
+	double kappa_star;
+	double theta_star;
+	double corner_x1;
+	double corner_x2;
+	double mu_ave;
+	double alpha_error;
+	double root_half_length;
+	double mean_mass;
+	double mean_mass2;
+	double mean_mass2_ln_mass;
+	double kappa_star_actual;
+	double m_lower;
+	double m_upper;
+	double m_lower_actual;
+	double m_upper_actual;
+	double mean_mass_actual;
+	double mean_mass2_actual;
+	double mean_mass2_ln_mass_actual;
+	double max_error;            /* max_error_1/mu */
+	long long num_points;        /* num_roots * (num_phi + num_branches) */
+	long long root_updates;      /* executed Aberth updates */
+	long long sum_terms;         /* executed reciprocal-sum terms */
+	long long unconverged;       /* points whose sweep cap was reached */
+	int max_sweeps_init;         /* most sweeps any branch centre needed */
+	int max_sweeps_step;         /* most sweeps any phi step needed */
+	double t_stars;              /* seconds, CUDA events */
+	double t_tree;               /* tree build + FMM coefficients */
+	double t_init_roots;
+	double t_ccs;
+	double t_caustics;           /* residual, caustic map, length scales */
+	double t_total;              /* star generation -> caustics on the device */
+	long long kernel_launches;   /* CUDA kernels this field's run launched */
+	long long root_updates_init; /* the part of root_updates done at the branch centres */
+	long long sum_terms_init;    /* the part of sum_terms done at the branch centres */
+	double reserved[5];
+} ccf_info;
+
+typedef struct ccf_handle ccf_handle;
+
+/* Library version and ABI check. */
+int ccf_abi_version(void);
+
+/* Fill p with the reference's defaults (include/ccf.cuh:42-62). */
+void ccf_default_params(ccf_params* p);
+
+/* Replaces the CCF<T> default constructor (include/ccf.cuh:68-71). */
+ccf_status ccf_create(ccf_handle** out);
+
+/* Releases all device and host memory of the handle. */
+void ccf_destroy(ccf_handle* h);
+
+/* Replaces assignment to the public fields of CCF<T> (include/ccf.cuh:42-62). */
+ccf_status ccf_set_params(ccf_handle* h, const ccf_params* p);
+ccf_status ccf_get_params(const ccf_handle* h, ccf_params* p);
+
+/* Supply a star field in memory instead of a star file: the in-memory form of
+   -sf/--starfile (include/star.cuh:175-320).  xym holds n triples
+   (x1, x2, mass).  Pass n = 0 to go back to generated fields. */
+ccf_status ccf_set_stars(ccf_handle* h, int n, const double* xym, int rectangular,
+	double corner_x1, double corner_x2, double theta_star);
+
+/* Replaces bool CCF<T>::run(int verbose) (include/ccf.cuh:1265-1280):
+   star field, tree and FMM, initial roots, phi continuation, 1/mu errors,
+   caustics and (if requested) length scales, all resident on the device. */
+ccf_status ccf_run(ccf_handle* h, int verbose);
+
+/* Replaces bool CCF<T>::save(int verbose) (include/ccf.cuh:1282-1287):
+   writes ccf_parameter_info.txt and the requested .bin files with the
+   reference's layout (include/ccf.cuh:1123-1260). */
+ccf_status ccf_save(ccf_handle* h, int verbose);
+
+/* Derived parameters, statistics and timings of the last run. */
+ccf_status ccf_get_info(const ccf_handle* h, ccf_info* info);
+
+/* Copy results to host memory, in the reference's file layout
+   (include/ccf.cuh:1214-1257): rows = num_roots * num_branches,
+   cols = num_phi / num_branches + 1, row = root * num_branches + branch.
+   Complex arrays are interleaved (re, im) doubles.  Any pointer may be NULL.
+   stars: num_stars triples (x1, x2, mass) in tree order, as ccf_stars.bin. */
+ccf_status ccf_get_results(ccf_handle* h, double* ccs, double* caustics, double* errs,
+	double* mu_length_scales, double* stars);
+
+/* Device pointers of the same arrays (valid until the next run or destroy);
+   a pointer is NULL when that output was not requested. */
+ccf_status ccf_get_device_results(ccf_handle* h, const double** ccs, const double** caustics,
+	const double** errs, const double** mu_length_scales);
+
+/* Message of the last failure on this handle ("" if none). */
+const char* ccf_last_error(const ccf_handle* h);
+
+/* Checks p and computes the derived parameters (corner, taylor_smooth,
+   num_roots, mass-function moments) on the host; needs no GPU.
+   Restates include/ccf.cuh:218-497.  msg (may be NULL) receives the reason
+   of a CCF_ERR_INVALID_ARGUMENT. */
+ccf_status ccf_derive_params(const ccf_params* p, ccf_info* info, char* msg, size_t msg_len);
+
+/* Run several independent fields as one batch: their rows share persistent
+   solver launches (the reference handles one field per process).  handles[i]
+   carries the parameters of field i; results and info land in each handle. */
+ccf_status ccf_run_batch(ccf_handle** handles, int n, int verbose);
+
+/* Write the star file of the last run (include/star.cuh:498-534) to an
+   explicit path. */
+ccf_status ccf_write_star_file(const ccf_handle* h, const char* path);
+
+/* Evaluate the field of the last run at n host points z (interleaved
+   complex) with phases phi: the critical-curve function f and its
+   z-derivative (include/ccf_functions.cuh:69-121), the lens map w
+   (ccf_functions.cuh:33-45), the 1/mu error bound (ccf_functions.cuh:457-463)
+   and the length scale (ccf_functions.cuh:144-166).  These are the device
+   functions the reference's kernels call, exposed for checks and for
+   callers that need the map at arbitrary points.  Any output may be NULL. */
+ccf_status ccf_eval_points(ccf_handle* h, int n, const double* z, const double* phi, double* f, double* df,
+	double* w, double* err, double* mu_length);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CCF_GB300_H */

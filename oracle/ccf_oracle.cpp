@@ -1500,6 +1500,48 @@ int oracle_run(const oracle_params* p, oracle_info* info, double* stars_out,
 	return 0;
 }
 
+int oracle_match_index(int rows, int cols, int nb, const double* a, const double* b, int* idx, double* dist)
+{
+	if (rows % nb != 0) return 1;
+	const int R = rows / nb;
+#pragma omp parallel for schedule(dynamic, 4)
+	for (long long ck = 0; ck < (long long)nb * cols; ck++)
+	{
+		int c = (int)(ck / cols), k = (int)(ck % cols);
+		std::vector<std::pair<double, int>> bx(R);
+		std::vector<double> byy(R);
+		for (int r = 0; r < R; r++)
+		{
+			size_t ib = ((size_t)r * nb + c) * cols + k;
+			bx[r] = {b[2 * ib], r};
+			byy[r] = b[2 * ib + 1];
+		}
+		std::sort(bx.begin(), bx.end());
+		for (int r = 0; r < R; r++)
+		{
+			size_t ia = ((size_t)r * nb + c) * cols + k;
+			double ax = a[2 * ia], ay = a[2 * ia + 1];
+			int pos = (int)(std::lower_bound(bx.begin(), bx.end(), std::make_pair(ax, -1)) - bx.begin());
+			double best = std::numeric_limits<double>::infinity();
+			int bi = -1;
+			for (int dir = -1; dir <= 1; dir += 2)
+			{
+				for (int q = (dir < 0 ? pos - 1 : pos); q >= 0 && q < R; q += dir)
+				{
+					double dx = bx[q].first - ax;
+					if (dx * dx > best) break;
+					int j = bx[q].second;
+					double d2 = dx * dx + (byy[j] - ay) * (byy[j] - ay);
+					if (d2 < best) { best = d2; bi = j; }
+				}
+			}
+			idx[ia] = bi < 0 ? -1 : (int)((size_t)bi * nb + c);
+			dist[ia] = std::sqrt(best);
+		}
+	}
+	return 0;
+}
+
 int oracle_match_sets(int rows, int cols, int nb, const double* a, const double* b,
 	double* max_dist, long long* non_bijective_cols, long long* non_finite)
 {

@@ -139,6 +139,10 @@ int oracle_eval(const oracle_params* p, oracle_info* info, int npts, const doubl
 int oracle_match_sets(int rows, int cols, int nb, const double* a, const double* b,
 	double* max_dist, long long* non_bijective_cols, long long* non_finite);
 
+/* as oracle_match_sets, and also writes for every entry of a the row of b it
+   matched (idx: rows*cols ints, -1 where unmatched) and its distance (dist). */
+int oracle_match_index(int rows, int cols, int nb, const double* a, const double* b, int* idx, double* dist);
+
 #ifdef __cplusplus
 }
 #endif

@@ -159,7 +159,7 @@ def make_params(stars=None, **kw) -> tuple[OracleParams, object]:
     keep = None
     for k, v in kw.items():
         if k == "mass_function":
-            v = MASS_FUNCTIONS[str(v).lower()]
+            v = MASS_FUNCTIONS.get(str(v).lower(), -1)
         if not hasattr(p, k):
             raise KeyError(k)
         setattr(p, k, v)
@@ -238,6 +238,32 @@ def match_sets(a, b, nb: int) -> dict:
     if rc != 0:
         raise ValueError("bad shapes")
     return {"max_dist": md.value, "non_bijective_cols": nbij.value, "non_finite": nfin.value}
+
+
+def match_index(a, b, nb: int):
+    """For every entry of a, the row of b holding its nearest root in the same
+    (branch, phi) column, and that distance.  Use ``take_matched`` to bring any
+    per-point array of b into a's order."""
+    a = np.ascontiguousarray(a, dtype=np.complex128)
+    b = np.ascontiguousarray(b, dtype=np.complex128)
+    rows, cols = a.shape
+    idx = np.empty((rows, cols), dtype=np.int32)
+    dist = np.empty((rows, cols))
+    L = lib()
+    L.oracle_match_index.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                     ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int),
+                                     ctypes.POINTER(ctypes.c_double)]
+    rc = L.oracle_match_index(rows, cols, nb, _dp(a.view(np.float64)), _dp(b.view(np.float64)),
+                              idx.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _dp(dist))
+    if rc != 0:
+        raise ValueError("bad shapes")
+    return idx, dist
+
+
+def take_matched(arr, idx):
+    """arr (rows, cols) of b rearranged into a's order by match_index's idx."""
+    cols = np.arange(arr.shape[1])[None, :]
+    return arr[np.clip(idx, 0, None), cols]
 
 
 # ---- readers for the reference's output layout (reference util.py:28-103) ----

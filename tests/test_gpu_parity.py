@@ -1,0 +1,247 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle.
+
+Root sets are matched per (branch, phi) column by nearest neighbour.  The
+oracle restates the reference's FP64 algorithm; because the reference stops
+after fixed sweep counts and an early 1/mu test, its raw roots sit up to
+~1e-8 theta_star from the converged ones, so the strict comparison is against
+the oracle polished to convergence (|step| < 1e-13 theta_star):
+
+    roots, caustics        <= 1e-9 theta_star   (observed ~1e-14)
+    1/mu error bounds      <= 1e-9 at every point
+    length scales          relative 1e-6 on matched points
+
+and against the raw reference fixture on the points the reference itself
+converged.  The exact smooth-mass forms (approx = 0) make f discontinuous at
+the field edge, so the zero set Aberth reaches there depends on the sweep
+order; for those the test checks that every GPU root is a converged zero of
+the oracle's own function.
+"""
+import glob
+import json
+import os
+
+import numpy as np
+import pytest
+
+from ccf_gb300 import CCF, run_batch
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+ROOT_TOL = 1e-9
+CFG0 = dict(kappa_tot=0.3, kappa_star=0.3, shear=0.1, theta_star=1.0, mass_function="equal", rectangular=0,
+            num_stars=100, num_phi=100, num_branches=1, random_seed=1234)
+
+
+def gpu_run(cfg, precision="mixed", mu=1, **extra):
+    c = CCF(**cfg)
+    c.precision = precision
+    c.write_mu_length_scales = mu
+    for k, v in extra.items():
+        setattr(c, k, v)
+    assert c.run(-1), c.last_error()
+    return c, c.results()
+
+
+def polished(cfg, mu=True):
+    return O.run(num_threads=8, polish_tol=1e-13, polish_max_iters=80, want_mu=mu, **cfg)
+
+
+def load(path):
+    g = np.load(path)
+    return json.loads(str(g["params"])), {k: g[k] for k in g.files}
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_small_field_parity(precision):
+    c, r = gpu_run(CFG0, precision)
+    ref = polished(CFG0)
+    info = r["info"]
+    assert info["unconverged"] == 0 and info["has_nan"] == 0
+    m = O.match_sets(r["ccs"], ref["ccs"], 1)
+    assert m["non_finite"] == 0 and m["non_bijective_cols"] == 0
+    assert m["max_dist"] <= ROOT_TOL * CFG0["theta_star"]
+    mc = O.match_sets(r["caustics"], ref["caustics"], 1)
+    assert mc["max_dist"] <= ROOT_TOL * CFG0["theta_star"]
+    assert np.max(r["errs"]) <= 1e-9
+    idx, dist = O.match_index(r["ccs"], ref["ccs"], 1)
+    mu_ref = O.take_matched(ref["mu_length_scales"], idx)
+    np.testing.assert_allclose(r["mu_length_scales"], mu_ref, rtol=1e-6)
+    # the same tree and expansion order as the reference
+    assert info["tree_levels"] == ref["info"]["tree_levels"]
+    assert info["expansion_order"] == ref["info"]["expansion_order"]
+
+
+def test_runs_are_deterministic():
+    _, a = gpu_run(CFG0, "mixed")
+    _, b = gpu_run(CFG0, "mixed")
+    assert np.array_equal(a["ccs"], b["ccs"])
+    assert np.array_equal(a["caustics"], b["caustics"])
+    assert np.array_equal(a["stars"], b["stars"])
+
+
+@pytest.mark.parametrize("path", [p for p in GOLDEN if "exact" not in p],
+                         ids=[os.path.basename(p)[:-4] for p in GOLDEN if "exact" not in p])
+def test_golden_fields(path):
+    cfg, g = load(path)
+    _, r = gpu_run(cfg, "mixed")
+    ref = polished(cfg)
+    nb = cfg["num_branches"]
+    theta = r["info"]["theta_star"]
+    m = O.match_sets(r["ccs"], ref["ccs"], nb)
+    assert m["non_finite"] == 0 and m["non_bijective_cols"] == 0
+    assert m["max_dist"] <= ROOT_TOL * theta
+    # caustics: inside the convergence disc of the Taylor alpha_smooth the
+    # reference's arithmetic is accurate; outside it carries its own rounding
+    # noise, so those points get the looser bound
+    idx, dist = O.match_index(r["ccs"], ref["ccs"], nb)
+    w_ref = O.take_matched(ref["caustics"], idx)
+    corner = abs(complex(r["info"]["corner_x1"], r["info"]["corner_x2"]))
+    inside = (np.abs(r["ccs"]) < 0.9 * corner) | (cfg.get("rectangular", 0) == 0)
+    dw = np.abs(r["caustics"] - w_ref)
+    assert np.max(dw[inside]) <= ROOT_TOL * theta
+    assert np.max(dw) <= 1e-6 * theta
+    assert np.max(r["errs"]) <= 1e-9
+    # the raw reference fixture, on the points where the reference converged
+    gi, gd = O.match_index(r["ccs"], g["ccs"], nb)
+    ref_conv = np.abs(O.take_matched(ref["ccs"], O.match_index(g["ccs"], ref["ccs"], nb)[0]) - g["ccs"]) < 1e-11
+    ok = O.take_matched(ref_conv.astype(np.int8), gi).astype(bool)
+    assert ok.mean() > 0.5
+    assert np.max(gd[ok]) <= ROOT_TOL * theta
+
+
+@pytest.mark.parametrize("path", [p for p in GOLDEN if "exact" in p],
+                         ids=[os.path.basename(p)[:-4] for p in GOLDEN if "exact" in p])
+def test_exact_smooth_mass_fields_are_converged_zeros(path):
+    cfg, g = load(path)
+    c, r = gpu_run(cfg, "mixed")
+    nb = cfg["num_branches"]
+    cols = cfg["num_phi"] // nb + 1
+    half = cfg["num_phi"] // (2 * nb)
+    assert r["info"]["unconverged"] == 0
+    # phase of every output point (include/ccf_functions.cuh:338-344)
+    rows = r["ccs"].shape[0]
+    branch = np.arange(rows) % nb
+    k = np.arange(cols)
+    phi = np.pi / nb + branch[:, None] * 2 * np.pi / nb + (k[None, :] - half) * 2 * np.pi / cfg["num_phi"]
+    o = O.eval_field(r["ccs"].ravel(), phi.ravel(), **cfg)
+    f_abs = np.abs(o["f"])
+    assert np.max(f_abs) < 1e-9
+    np.testing.assert_allclose(o["w"], r["caustics"].ravel(), rtol=0, atol=1e-9)
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_field_evaluation_matches_oracle(path):
+    cfg, g = load(path)
+    c, r = gpu_run(cfg, "mixed", mu=0)
+    rng = np.random.default_rng(7)
+    corner = abs(complex(r["info"]["corner_x1"], r["info"]["corner_x2"]))
+    rad = 0.8 * corner * np.sqrt(rng.uniform(0, 1, 2000))
+    z = rad * np.exp(2j * np.pi * rng.uniform(0, 1, 2000))
+    z = np.concatenate([z, r["ccs"].ravel()[:1000]])
+    phi = rng.uniform(0, 2 * np.pi, z.shape[0])
+    e = c.eval_points(z, phi)
+    o = O.eval_field(z, phi, **cfg)
+    scale = 1 + np.abs(o["f"])
+    assert np.max(np.abs(e["f"] - o["f"]) / scale) < 1e-11
+    assert np.max(np.abs(e["df"] - o["df"]) / (1 + np.abs(o["df"]))) < 1e-10
+    assert np.max(np.abs(e["w"] - o["w"]) / (1 + np.abs(o["w"]))) < 1e-11
+
+
+def test_generated_stars_match_the_reference_stream():
+    for path in GOLDEN:
+        cfg, g = load(path)
+        _, r = gpu_run(cfg, "mixed", mu=0, max_iters_init=1, max_iters_step=1)
+        a = np.sort(g["stars_generated"].copy().view("f8,f8,f8"), axis=0).view(np.float64).reshape(-1, 3)
+        b = np.sort(r["stars"].copy().view("f8,f8,f8"), axis=0).view(np.float64).reshape(-1, 3)
+        # device and host libm may differ in the last bits of pow/sin/cos; masses from the
+        # inverse CDF amplify that through a cancelling sum to ~1e-14 relative
+        np.testing.assert_allclose(b, a, rtol=1e-12, atol=0)
+
+
+def test_star_input_matches_generated_field():
+    c1, r1 = gpu_run(CFG0, "mixed", mu=0)
+    stars = r1["stars"]
+    inf = r1["info"]
+    c2 = CCF(**CFG0)
+    c2.set_stars(stars, 0, complex(inf["corner_x1"], inf["corner_x2"]), 1.0)
+    assert c2.run(-1), c2.last_error()
+    r2 = c2.results()
+    m = O.match_sets(r2["ccs"], r1["ccs"], 1)
+    assert m["max_dist"] <= 1e-12 and m["non_bijective_cols"] == 0
+
+
+def test_precisions_agree():
+    cfg = json.loads(str(np.load(GOLDEN[-1])["params"]))
+    _, a = gpu_run(cfg, "mixed", mu=0)
+    _, b = gpu_run(cfg, "fp64", mu=0)
+    m = O.match_sets(a["ccs"], b["ccs"], cfg["num_branches"])
+    assert m["max_dist"] <= 1e-11 and m["non_bijective_cols"] == 0
+
+
+def test_batch_equals_solo():
+    cfgs = [json.loads(str(np.load(p)["params"])) for p in GOLDEN if "exact" not in p]
+    solo = [gpu_run(c, "mixed", mu=0)[1] for c in cfgs]
+    fields = []
+    for cfg in cfgs:
+        f = CCF(**cfg)
+        f.write_mu_length_scales = 0
+        fields.append(f)
+    assert run_batch(fields, -1)
+    for f, s in zip(fields, solo):
+        r = f.results()
+        assert np.array_equal(r["ccs"], s["ccs"])
+        assert np.array_equal(r["caustics"], s["caustics"])
+
+
+def test_save_writes_the_reference_layout(tmp_path):
+    c, r = gpu_run(CFG0, "mixed", mu=1)
+    c.outfile_prefix = str(tmp_path) + "/"
+    assert c.save(-1), c.last_error()
+    ccs = O.read_array(str(tmp_path / "ccf_ccs.bin"), is_complex=True)
+    assert ccs.shape == (200, 101) and np.array_equal(ccs, r["ccs"])
+    w = O.read_array(str(tmp_path / "ccf_caustics.bin"), is_complex=True)
+    assert np.array_equal(w, r["caustics"])
+    mu = O.read_array(str(tmp_path / "ccf_mu_length_scales.bin"))
+    assert np.array_equal(mu, r["mu_length_scales"])
+    sf = O.read_star_file(str(tmp_path / "ccf_stars.bin"))
+    assert sf["stars"].shape == (100, 3) and sf["rectangular"] == 0
+    assert abs(sf["corner"].real - np.hypot(r["info"]["corner_x1"], r["info"]["corner_x2"])) < 1e-12
+    params = O.read_params(str(tmp_path / "ccf_parameter_info.txt"))
+    assert params["num_roots"] == 200 and params["num_phi"] == 100 and params["random_seed"] == 1234
+    keys = [line.split()[0] for line in open(tmp_path / "ccf_parameter_info.txt")]
+    assert keys[:6] == ["kappa_tot", "shear", "mu_ave", "smooth_fraction", "kappa_star", "kappa_star_actual"]
+    assert keys[-4:] == ["max_error_1/mu", "t_init_roots", "t_ccs", "t_caustics"]
+    # a field read back from the written star file gives the same curves
+    c2 = CCF(**CFG0)
+    c2.starfile = str(tmp_path / "ccf_stars.bin")
+    assert c2.run(-1), c2.last_error()
+    m = O.match_sets(c2.results()["ccs"], r["ccs"], 1)
+    assert m["max_dist"] <= 1e-12
+
+
+CFG1 = dict(kappa_tot=0.45, kappa_star=0.35, shear=0.35, theta_star=1, mass_function="salpeter", m_lower=0.08,
+            m_upper=1.5, m_solar=4.954984, rectangular=1, approx=1, num_stars=2000, num_phi=2048,
+            num_branches=32, random_seed=1235)
+
+
+def test_full_size_single_field_properties():
+    """2000 Salpeter stars, rectangular field with smooth mass, 2048 phi steps
+    over 32 branches: every point converged and finite, every 1/mu bound below
+    the tolerance, and a sample of columns equal to the polished oracle."""
+    c, r = gpu_run(CFG1, "mixed", mu=0)
+    info = r["info"]
+    assert info["unconverged"] == 0 and info["has_nan"] == 0
+    assert np.isfinite(r["ccs"]).all() and np.isfinite(r["caustics"]).all()
+    assert np.max(r["errs"]) <= 1e-9
+    # oracle on a bounded sample: branch 0, centre and the first step each side
+    ref = O.run(num_threads=16, max_branches=1, max_steps=1, polish_tol=1e-13, polish_max_iters=80, **CFG1)
+    nb = CFG1["num_branches"]
+    half = CFG1["num_phi"] // (2 * nb)
+    rows = slice(0, None, nb)
+    cols = [half - 1, half, half + 1]
+    a = r["ccs"][rows][:, cols]
+    b = ref["ccs"][rows][:, cols]
+    m = O.match_sets(a, b, 1)
+    assert m["non_bijective_cols"] == 0 and m["max_dist"] <= ROOT_TOL
