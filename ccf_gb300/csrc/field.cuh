@@ -213,51 +213,107 @@ CCF_D double2 smooth_alpha(const FieldView& F, double2 z)
 
 /* ---------------- star + local terms ---------------- */
 
-/* Accumulates over the near stars of the leaf (or all stars when leaf < 0):
-   s1 = sum m / d, s2 = sum m / d^2, s3 = sum m / d^3 with d = z - z_i. */
-template <bool NEED1, bool NEED3>
-CCF_D void near_sums(const FieldView& F, int leaf, double2 z, double2& s1, double2& s2, double2& s3)
+/* sums over stars of m / d^k, d = z - z_i: s1 (k = 1), s2 (k = 2), s3 (k = 3) */
+struct NearSums
 {
-	s1 = make_double2(0, 0);
-	s2 = make_double2(0, 0);
-	s3 = make_double2(0, 0);
-	auto body = [&](double sx, double sy, double m) {
-		double dx = z.x - sx, dy = z.y - sy;
-		double r = rcp64(dx * dx + dy * dy);
-		double ix = dx * r, iy = -dy * r;             /* 1/d */
-		double i2x = ix * ix - iy * iy, i2y = 2 * ix * iy;  /* 1/d^2 */
-		s2.x = fma(m, i2x, s2.x);
-		s2.y = fma(m, i2y, s2.y);
-		if (NEED1)
-		{
-			s1.x = fma(m, ix, s1.x);
-			s1.y = fma(m, iy, s1.y);
-		}
-		if (NEED3)
-		{
-			double i3x = i2x * ix - i2y * iy, i3y = i2x * iy + i2y * ix;
-			s3.x = fma(m, i3x, s3.x);
-			s3.y = fma(m, i3y, s3.y);
-		}
-	};
-	if (leaf >= 0)
+	double2 s1, s2, s3;
+};
+
+template <bool NEED1, bool NEED3>
+CCF_D void star_term(NearSums& a, double2 z, double sx, double sy, double m)
+{
+	double dx = z.x - sx, dy = z.y - sy;
+	double r = rcp64(dx * dx + dy * dy);
+	double ix = dx * r, iy = -dy * r;                   /* 1/d */
+	double i2x = ix * ix - iy * iy, i2y = 2 * ix * iy;  /* 1/d^2 */
+	a.s2.x = fma(m, i2x, a.s2.x);
+	a.s2.y = fma(m, i2y, a.s2.y);
+	if (NEED1)
 	{
-		int n = F.leaf_near_count[leaf];
-		const NearStar* ns = F.leaf_near + (size_t)leaf * MAX_NEAR;
-		for (int i = 0; i < n; i++)
-		{
-			NearStar s = ns[i];
-			body(s.x, s.y, s.m);
-		}
+		a.s1.x = fma(m, ix, a.s1.x);
+		a.s1.y = fma(m, iy, a.s1.y);
 	}
-	else
+	if (NEED3)
 	{
-		for (int i = 0; i < F.num_stars; i++)
+		double i3x = i2x * ix - i2y * iy, i3y = i2x * iy + i2y * ix;
+		a.s3.x = fma(m, i3x, a.s3.x);
+		a.s3.y = fma(m, i3y, a.s3.y);
+	}
+}
+
+CCF_D NearSums zero_sums()
+{
+	NearSums a;
+	a.s1 = make_double2(0, 0);
+	a.s2 = make_double2(0, 0);
+	a.s3 = make_double2(0, 0);
+	return a;
+}
+
+/* direct sums over the <= 32 stars of a leaf and its neighbours
+   (include/alpha_star.cuh:18-115) */
+template <bool NEED1, bool NEED3>
+CCF_D NearSums leaf_sums(const FieldView& F, int leaf, double2 z)
+{
+	NearSums a = zero_sums();
+	int n = F.leaf_near_count[leaf];
+	const NearStar* ns = F.leaf_near + (size_t)leaf * MAX_NEAR;
+	for (int i = 0; i < n; i++)
+	{
+		NearStar s = ns[i];
+		star_term<NEED1, NEED3>(a, z, s.x, s.y, s.m);
+	}
+	return a;
+}
+
+/* Off-field points (outside the root box) take the direct sum over every
+   star, as the reference does when the root is the nearest node
+   (include/tree_node.cuh:535-539).  The warp computes those sums together:
+   every lane takes every 32nd star for one off-field point at a time, so one
+   such point costs the warp N/32 terms instead of N.  Must be called by all
+   32 lanes; lanes with need set receive their sums in out. */
+template <bool NEED1, bool NEED3>
+CCF_D void offfield_sums_warp(const FieldView& F, bool need, double2 z, NearSums& out)
+{
+	const unsigned full = 0xffffffffu;
+	const int lane = threadIdx.x & 31;
+	unsigned m = __ballot_sync(full, need);
+	while (m)
+	{
+		int src = __ffs(m) - 1;
+		m &= m - 1;
+		double2 zz = make_double2(__shfl_sync(full, z.x, src), __shfl_sync(full, z.y, src));
+		NearSums a = zero_sums();
+		for (int i = lane; i < F.num_stars; i += 32)
 		{
 			double2 p = F.star_pos[i];
-			body(p.x, p.y, F.star_mass[i]);
+			star_term<NEED1, NEED3>(a, zz, p.x, p.y, F.star_mass[i]);
+		}
+		double v[6] = {a.s1.x, a.s1.y, a.s2.x, a.s2.y, a.s3.x, a.s3.y};
+#pragma unroll
+		for (int k = 0; k < 6; k++)
+		{
+			for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(full, v[k], o);
+		}
+		if (lane == src)
+		{
+			out.s1 = make_double2(v[0], v[1]);
+			out.s2 = make_double2(v[2], v[3]);
+			out.s3 = make_double2(v[4], v[5]);
 		}
 	}
+}
+
+/* near sums for one point per lane: its leaf's direct sum, or (off-field)
+   the warp-cooperative sum over all stars.  All lanes must call it; lanes
+   with active false contribute nothing and get zeros. */
+template <bool NEED1, bool NEED3>
+CCF_D NearSums point_sums_warp(const FieldView& F, bool active, int leaf, double2 z)
+{
+	NearSums a = zero_sums();
+	if (active && leaf >= 0) a = leaf_sums<NEED1, NEED3>(F, leaf, z);
+	offfield_sums_warp<NEED1, NEED3>(F, active && leaf < 0, z, a);
+	return a;
 }
 
 /* Horner of the pre-scaled local coefficients: sum_{i >= first} L[i] dz^(i - first) */
@@ -278,22 +334,21 @@ CCF_D double2 leaf_dz(const FieldView& F, int leaf, double2 z)
 /* parametric critical-curve function f(z; phi) (ccf_functions.cuh:69-86):
    f = gamma - conj(dalpha_star/dzbar) - conj(dalpha_local/dzbar)
        - conj(dalpha_smooth/dzbar) - (1 - kappa - dalpha_smooth/dz) e^{-i phi}
-   and, when DF is true, its z derivative (ccf_functions.cuh:108-121). */
+   from the star sums S, and, when DF is true, its z derivative
+   (ccf_functions.cuh:108-121). */
 template <bool DF>
-CCF_D void eval_f64(const FieldView& F, int leaf, double2 z, double cphi, double sphi, double2& f, double2& df)
+CCF_D void eval_f64(const FieldView& F, int leaf, double2 z, double cphi, double sphi, const NearSums& S, double2& f, double2& df)
 {
-	double2 s1, s2, s3;
-	near_sums<false, DF>(F, leaf, z, s1, s2, s3);
 	/* -conj(d alpha_star / d zbar) = theta^2 sum m / d^2 */
-	f = make_double2(F.shear + F.theta2 * s2.x, F.theta2 * s2.y);
+	f = make_double2(F.shear + F.theta2 * S.s2.x, F.theta2 * S.s2.y);
 	double2 dl = make_double2(0, 0), d2l = make_double2(0, 0);
-	if (leaf >= 0 && F.order >= 2)
+	if (leaf >= 0)
 	{
 		const int P = F.order;
 		double2 dz = leaf_dz(F, leaf, z);
 		const double2* L = F.leaf_loc + (size_t)leaf * 3 * (P + 1);
 		dl = local_horner(L + (P + 1), P, 2, dz);
-		if (DF && P >= 3) d2l = local_horner(L + 2 * (P + 1), P, 3, dz);
+		if (DF) d2l = local_horner(L + 2 * (P + 1), P, 3, dz);
 	}
 	double2 ds = smooth_dzbar(F, z);
 	double sz = smooth_dz(F, z);
@@ -305,24 +360,17 @@ CCF_D void eval_f64(const FieldView& F, int leaf, double2 z, double cphi, double
 		double2 d2s = smooth_d2zbar(F, z);
 		/* f' = -conj(d2 alpha_star) - conj(d2 alpha_local) - conj(d2 alpha_smooth)
 		      = -2 theta^2 sum m / d^3 - H3 - conj(d2s) */
-		df.x = -2 * F.theta2 * s3.x - d2l.x - d2s.x;
-		df.y = -2 * F.theta2 * s3.y - d2l.y + d2s.y;
+		df.x = -2 * F.theta2 * S.s3.x - d2l.x - d2s.x;
+		df.y = -2 * F.theta2 * S.s3.y - d2l.y + d2s.y;
 	}
 }
 
 /* f'(z) in FP32 for the mixed-precision solver: only the step size depends
-   on it, never the converged root. */
-CCF_D float2 eval_df32(const FieldView& F, int leaf, double2 z)
+   on it, never the converged root.  Off-field points use the FP64 s3 of the
+   warp-cooperative sum. */
+CCF_D float2 eval_df32(const FieldView& F, int leaf, double2 z, double2 s3_off)
 {
 	float2 s3 = make_float2(0, 0);
-	auto body = [&](float dx, float dy, float m) {
-		float r = rcp32(dx * dx + dy * dy);
-		float ix = dx * r, iy = -dy * r;
-		float i2x = ix * ix - iy * iy, i2y = 2 * ix * iy;
-		float i3x = i2x * ix - i2y * iy, i3y = i2x * iy + i2y * ix;
-		s3.x = fmaf(m, i3x, s3.x);
-		s3.y = fmaf(m, i3y, s3.y);
-	};
 	float2 d2l = make_float2(0, 0);
 	if (leaf >= 0)
 	{
@@ -331,26 +379,25 @@ CCF_D float2 eval_df32(const FieldView& F, int leaf, double2 z)
 		for (int i = 0; i < n; i++)
 		{
 			NearStar s = ns[i];
-			body((float)(z.x - s.x), (float)(z.y - s.y), (float)s.m);
+			float dx = (float)(z.x - s.x), dy = (float)(z.y - s.y), m = (float)s.m;
+			float r = rcp32(dx * dx + dy * dy);
+			float ix = dx * r, iy = -dy * r;
+			float i2x = ix * ix - iy * iy, i2y = 2 * ix * iy;
+			float i3x = i2x * ix - i2y * iy, i3y = i2x * iy + i2y * ix;
+			s3.x = fmaf(m, i3x, s3.x);
+			s3.y = fmaf(m, i3y, s3.y);
 		}
 		const int P = F.order;
-		if (P >= 3)
-		{
-			double2 dzd = leaf_dz(F, leaf, z);
-			float2 dz = make_float2((float)dzd.x, (float)dzd.y);
-			const float2* L = F.leaf_loc3f + (size_t)leaf * (P + 1);
-			float2 acc = L[P];
-			for (int i = P - 1; i >= 3; i--) acc = fadd(fmulc(acc, dz), L[i]);
-			d2l = acc;
-		}
+		double2 dzd = leaf_dz(F, leaf, z);
+		float2 dz = make_float2((float)dzd.x, (float)dzd.y);
+		const float2* L = F.leaf_loc3f + (size_t)leaf * (P + 1);
+		float2 acc = L[P];
+		for (int i = P - 1; i >= 3; i--) acc = fadd(fmulc(acc, dz), L[i]);
+		d2l = acc;
 	}
 	else
 	{
-		for (int i = 0; i < F.num_stars; i++)
-		{
-			double2 p = F.star_pos[i];
-			body((float)(z.x - p.x), (float)(z.y - p.y), (float)F.star_mass[i]);
-		}
+		s3 = make_float2((float)s3_off.x, (float)s3_off.y);
 	}
 	float2 d2s;
 	if (F.rectangular && F.approx && F.smooth_m > 0)
@@ -376,7 +423,7 @@ CCF_D float2 eval_df32(const FieldView& F, int leaf, double2 z)
 /* everything the epilogue needs at a final root: the 1/mu error bound
    (ccf_functions.cuh:419-467), the caustic w = (1 - kappa) z + gamma zbar
    - alpha (ccf_functions.cuh:33-45) and the magnification length scale
-   (ccf_functions.cuh:144-166). */
+   (ccf_functions.cuh:144-166), from the star sums S of the point. */
 struct PointResult
 {
 	double err;
@@ -385,28 +432,25 @@ struct PointResult
 };
 
 template <bool WANT_W, bool WANT_MU>
-CCF_D PointResult eval_point(const FieldView& F, double2 z, double cphi, double sphi)
+CCF_D PointResult eval_point(const FieldView& F, int leaf, double2 z, double cphi, double sphi, const NearSums& S)
 {
-	int leaf = find_leaf(F, z);
-	double2 s1, s2, s3;
-	near_sums<true, WANT_MU>(F, leaf, z, s1, s2, s3);
 	const int P = F.order;
 	double2 al = make_double2(0, 0), dl = make_double2(0, 0), d2l = make_double2(0, 0);
 	if (leaf >= 0)
 	{
 		double2 dz = leaf_dz(F, leaf, z);
 		const double2* L = F.leaf_loc + (size_t)leaf * 3 * (P + 1);
-		if (P >= 1) al = local_horner(L, P, 1, dz);
-		if (P >= 2) dl = local_horner(L + (P + 1), P, 2, dz);
-		if (WANT_MU && P >= 3) d2l = local_horner(L + 2 * (P + 1), P, 3, dz);
+		if (WANT_W) al = local_horner(L, P, 1, dz);
+		dl = local_horner(L + (P + 1), P, 2, dz);
+		if (WANT_MU) d2l = local_horner(L + 2 * (P + 1), P, 3, dz);
 	}
 	double2 ds = smooth_dzbar(F, z);
 	double sz = smooth_dz(F, z);
 	double a = 1 - F.kappa_tot - sz;
 	/* f0 and the 1/mu bound */
 	double2 f;
-	f.x = F.shear + F.theta2 * s2.x - dl.x - ds.x - a * cphi;
-	f.y = F.theta2 * s2.y - dl.y + ds.y + a * sphi;
+	f.x = F.shear + F.theta2 * S.s2.x - dl.x - ds.x - a * cphi;
+	f.y = F.theta2 * S.s2.y - dl.y + ds.y + a * sphi;
 	double af = hypot(f.x, f.y);
 	PointResult out;
 	double e1 = fabs(af * (af + 2 * a));
@@ -416,8 +460,8 @@ CCF_D PointResult eval_point(const FieldView& F, double2 z, double cphi, double 
 	{
 		/* alpha_star = theta^2 conj(s1), alpha_local = conj(H1) */
 		double2 as = smooth_alpha(F, z);
-		out.w.x = (1 - F.kappa_tot) * z.x + F.shear * z.x - F.theta2 * s1.x - al.x - as.x;
-		out.w.y = (1 - F.kappa_tot) * z.y - F.shear * z.y + F.theta2 * s1.y + al.y - as.y;
+		out.w.x = (1 - F.kappa_tot) * z.x + F.shear * z.x - F.theta2 * S.s1.x - al.x - as.x;
+		out.w.y = (1 - F.kappa_tot) * z.y - F.shear * z.y + F.theta2 * S.s1.y + al.y - as.y;
 	}
 	else
 	{
@@ -427,14 +471,14 @@ CCF_D PointResult eval_point(const FieldView& F, double2 z, double cphi, double 
 	{
 		/* dw/dzbar = gamma - dalpha_star/dzbar - dalpha_local/dzbar - dalpha_smooth/dzbar */
 		double2 dwdzb;
-		dwdzb.x = F.shear + F.theta2 * s2.x - dl.x - ds.x;
-		dwdzb.y = -F.theta2 * s2.y + dl.y - ds.y;
+		dwdzb.x = F.shear + F.theta2 * S.s2.x - dl.x - ds.x;
+		dwdzb.y = -F.theta2 * S.s2.y + dl.y - ds.y;
 		double2 d2s = smooth_d2zbar(F, z);
 		/* d2w/dzbar2 = -(d2 alpha_star) - (d2 alpha_local) - (d2 alpha_smooth);
 		   d2 alpha_star = 2 theta^2 conj(s3), d2 alpha_local = conj(H3) */
 		double2 d2w;
-		d2w.x = -2 * F.theta2 * s3.x - d2l.x - d2s.x;
-		d2w.y = 2 * F.theta2 * s3.y + d2l.y - d2s.y;
+		d2w.x = -2 * F.theta2 * S.s3.x - d2l.x - d2s.x;
+		d2w.y = 2 * F.theta2 * S.s3.y + d2l.y - d2s.y;
 		double2 cct = cmul(cmul(make_double2(0, -2), cconj(dwdzb)), d2w);
 		double2 ct = cadd(cscale(cct, a), cmul(dwdzb, cconj(cct)));
 		out.mu_length = 1 / (2 * hypot(ct.x, ct.y));

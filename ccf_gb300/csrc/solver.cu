@@ -69,15 +69,22 @@ CCF_D double row_phi(int c, int nb, int nphi, int side, int j)
 	return side == 0 ? phi0 - dphi : phi0 + dphi;
 }
 
-/* One Aberth step of root a given its correction sum S; returns false when
-   the step is not finite (the root is then frozen).  Not inlined: the FP64
-   evaluation needs many registers once, not once per unrolled target. */
+/* One Aberth step for the target of every lane with valid set, given its
+   correction sum S; returns 0, 1 when the root became final, 2 when the step
+   was not finite (the root is then frozen).  All 32 lanes of the warp must
+   call it: off-field targets take their star sums from the whole warp.  Not
+   inlined: the FP64 evaluation needs its registers once, not once per
+   unrolled target. */
 template <bool MIXED>
-__device__ __noinline__ bool aberth_update(const FieldView& F, double2* __restrict__ master, unsigned char* __restrict__ fin,
-	int a, double2 S, bool disc_exact, double cphi, double sphi)
+__device__ __noinline__ int aberth_update_warp(const FieldView& F, double2* __restrict__ master, unsigned char* __restrict__ fin,
+	bool valid, int a, double2 S, bool disc_exact, double cphi, double sphi)
 {
-	double2 z = master[a];
-	int leaf = find_leaf(F, z);
+	double2 z = valid ? master[a] : make_double2(0, 0);
+	int leaf = valid ? find_leaf(F, z) : 0;
+	NearSums ns = zero_sums();
+	if (valid && leaf >= 0) ns = leaf_sums<false, !MIXED>(F, leaf, z);
+	offfield_sums_warp<false, true>(F, valid && leaf < 0, z, ns);
+	if (!valid) return 0;
 	if (disc_exact)
 	{
 		double2 iz = cinv(z);
@@ -87,40 +94,51 @@ __device__ __noinline__ bool aberth_update(const FieldView& F, double2* __restri
 	double2 f, df;
 	if constexpr (MIXED)
 	{
-		eval_f64<false>(F, leaf, z, cphi, sphi, f, df);
-		float2 d32 = eval_df32(F, leaf, z);
+		eval_f64<false>(F, leaf, z, cphi, sphi, ns, f, df);
+		float2 d32 = eval_df32(F, leaf, z, ns.s3);
 		df = make_double2(d32.x, d32.y);
 	}
 	else
 	{
-		eval_f64<true>(F, leaf, z, cphi, sphi, f, df);
+		eval_f64<true>(F, leaf, z, cphi, sphi, ns, f, df);
 	}
 	double2 den = cadd(df, cmul(f, S));
 	double2 znew = csub(z, cdiv(f, den));
 	if (isfinite(znew.x) && isfinite(znew.y))
 	{
 		double norm = hypot(znew.x - z.x, znew.y - z.y) / F.theta;
-		if (norm < 0.000000001) fin[a] = 1;
 		master[a] = znew;
-		return true;
+		if (norm < 0.000000001)
+		{
+			fin[a] = 1;
+			return 1;
+		}
+		return 0;
 	}
 	fin[a] = 1;
-	return false;
+	return 2;
 }
 
-/* outputs of one final root: position, 1/mu bound, caustic, length scale */
-__device__ __noinline__ void point_epilogue(const FieldView& F, const FieldOut& O, double2 z, size_t out, double cphi, double sphi,
-	double* maxerr, int* nan)
+/* outputs of one final root per lane: position, 1/mu bound, caustic,
+   length scale.  All 32 lanes must call it (see aberth_update_warp). */
+__device__ __noinline__ void point_epilogue_warp(const FieldView& F, const FieldOut& O, bool valid, double2 z, size_t out,
+	double cphi, double sphi, double* maxerr, int* nan)
 {
+	int leaf = valid ? find_leaf(F, z) : 0;
+	NearSums ns = zero_sums();
+	const bool mu = O.mu != nullptr;
+	if (valid && leaf >= 0) ns = mu ? leaf_sums<true, true>(F, leaf, z) : leaf_sums<true, false>(F, leaf, z);
+	offfield_sums_warp<true, true>(F, valid && leaf < 0, z, ns);
+	if (!valid) return;
 	PointResult pr;
-	if (O.caustics && O.mu) pr = eval_point<true, true>(F, z, cphi, sphi);
-	else if (O.caustics) pr = eval_point<true, false>(F, z, cphi, sphi);
-	else if (O.mu) pr = eval_point<false, true>(F, z, cphi, sphi);
-	else pr = eval_point<false, false>(F, z, cphi, sphi);
+	if (O.caustics && mu) pr = eval_point<true, true>(F, leaf, z, cphi, sphi, ns);
+	else if (O.caustics) pr = eval_point<true, false>(F, leaf, z, cphi, sphi, ns);
+	else if (mu) pr = eval_point<false, true>(F, leaf, z, cphi, sphi, ns);
+	else pr = eval_point<false, false>(F, leaf, z, cphi, sphi, ns);
 	O.ccs[out] = z;
 	O.errs[out] = pr.err;
 	if (O.caustics) O.caustics[out] = pr.w;
-	if (O.mu) O.mu[out] = pr.mu_length;
+	if (mu) O.mu[out] = pr.mu_length;
 	if (isfinite(pr.err)) atomicMax((unsigned long long*)maxerr, (unsigned long long)__double_as_longlong(pr.err));
 	else atomicOr(nan, 1);
 }
@@ -345,13 +363,13 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 					__syncthreads();
 				}
 
-				/* the Aberth update of each target */
+				/* the Aberth update of each target (warp-uniform calls) */
 #pragma unroll
 				for (int t = 0; t < TPT; t++)
 				{
-					if (!valid[t]) continue;
 					double2 S = make_double2(2 * totS[t].x - totR[t].x, 2 * totS[t].y - totR[t].y);
-					if (!aberth_update<MIXED>(F, master, fin, tid_a[t], S, disc_exact, cphi, sphi)) atomicOr(&s_nan, 2);
+					if (aberth_update_warp<MIXED>(F, master, fin, valid[t], tid_a[t], S, disc_exact, cphi, sphi) == 2)
+						atomicOr(&s_nan, 2);
 				}
 			}
 			if (threadIdx.x == 0)
@@ -377,11 +395,15 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 
 		/* epilogue: outputs of this phi step for the roots this CTA owns */
 		const int k = initial ? sO.half : (side == 0 ? sO.half - j : sO.half + j);
-		for (int a = o0 + threadIdx.x; a < o1; a += NT)
+		for (int a0 = o0; a0 < o1; a0 += NT)
 		{
-			double2 z = master[a];
-			size_t out = ((size_t)a * nb + c) * sO.cols + k;
-			point_epilogue(F, sO, z, out, cphi, sphi, &s_maxerr, &s_nan);
+			/* uniform trip count: the epilogue is a warp-wide call */
+			const int a = a0 + threadIdx.x;
+			const bool v = a < o1;
+			double2 z = v ? master[a] : make_double2(0, 0);
+			size_t out = ((size_t)(v ? a : 0) * nb + c) * sO.cols + k;
+			point_epilogue_warp(F, sO, v, z, out, cphi, sphi, &s_maxerr, &s_nan);
+			if (!v) continue;
 			if (!fin[a]) atomicAdd(&s_unconv, 1ull);
 			if (initial)
 			{
@@ -454,18 +476,23 @@ cudaError_t launch_solve(cudaStream_t s, const SolveArgs& a, bool mixed, bool in
 __global__ void eval_points_kernel(const FieldView* __restrict__ Fp, int npts, const double2* __restrict__ z,
 	const double* __restrict__ phi, double2* f, double2* df, double2* w, double* err, double* mu)
 {
+	/* every lane of a warp stays to the end: off-field sums are warp-wide */
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= npts) return;
+	const bool v = i < npts;
 	const FieldView F = *Fp;
-	double2 zz = z[i];
+	double2 zz = v ? z[i] : make_double2(0, 0);
 	double sp, cp;
-	sincos(phi[i], &sp, &cp);
-	int leaf = find_leaf(F, zz);
+	sincos(v ? phi[i] : 0.0, &sp, &cp);
+	int leaf = v ? find_leaf(F, zz) : 0;
+	NearSums ns = zero_sums();
+	if (v && leaf >= 0) ns = leaf_sums<true, true>(F, leaf, zz);
+	offfield_sums_warp<true, true>(F, v && leaf < 0, zz, ns);
+	if (!v) return;
 	double2 fv, dv;
-	eval_f64<true>(F, leaf, zz, cp, sp, fv, dv);
+	eval_f64<true>(F, leaf, zz, cp, sp, ns, fv, dv);
 	if (f) f[i] = fv;
 	if (df) df[i] = dv;
-	PointResult pr = eval_point<true, true>(F, zz, cp, sp);
+	PointResult pr = eval_point<true, true>(F, leaf, zz, cp, sp, ns);
 	if (w) w[i] = pr.w;
 	if (err) err[i] = pr.err;
 	if (mu) mu[i] = pr.mu_length;
