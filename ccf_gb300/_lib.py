@@ -113,6 +113,7 @@ EXPORTED = [
     "ccf_abi_version", "ccf_default_params", "ccf_create", "ccf_destroy", "ccf_set_params", "ccf_get_params",
     "ccf_set_stars", "ccf_run", "ccf_save", "ccf_get_info", "ccf_get_results", "ccf_get_device_results",
     "ccf_last_error", "ccf_derive_params", "ccf_run_batch", "ccf_write_star_file", "ccf_eval_points",
+    "ccf_continue_branch_noalloc",
 ]
 
 _lib = None
@@ -153,6 +154,8 @@ def load(path: str | None = None):
         L.ccf_run_batch.argtypes = [ctypes.POINTER(H), ctypes.c_int, ctypes.c_int]
         L.ccf_write_star_file.argtypes = [H, ctypes.c_char_p]
         L.ccf_eval_points.argtypes = [H, ctypes.c_int, dp, dp, dp, dp, dp, dp, dp]
+        vp = ctypes.c_void_p
+        L.ccf_continue_branch_noalloc.argtypes = [H, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp]
         for name in EXPORTED:
             fn = getattr(L, name)
             if fn.restype is ctypes.c_int and name not in ("ccf_abi_version",):

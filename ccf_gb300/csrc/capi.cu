@@ -17,6 +17,10 @@ struct ccf_handle
 	std::string last_error;
 };
 
+ccf::Field* ccf_internal_field(ccf_handle* h) { return &h->field; }
+ccf::Engine* ccf_internal_engine(ccf_handle* h) { return &h->engine; }
+void ccf_internal_set_error(ccf_handle* h, const std::string& msg) { h->last_error = msg; }
+
 static ccf_status fail(ccf_handle* h, ccf_status s, const std::string& msg)
 {
 	if (h) h->last_error = msg;

@@ -218,6 +218,28 @@ ccf_status ccf_write_star_file(const ccf_handle* h, const char* path);
 ccf_status ccf_eval_points(ccf_handle* h, int n, const double* z, const double* phi, double* f, double* df,
 	double* w, double* err, double* mu_length);
 
+/* Continue one (branch, side) of the field built by the last ccf_run on h,
+   from caller-supplied starting roots, without allocating any device memory.
+   This entry point has no counterpart in the reference.  It exists for
+   callers that cannot call cudaMalloc where they need the extra phi steps: a
+   host framework that owns all device memory through its own pool, or a
+   real-time loop that must not take the allocator's locks or synchronise
+   implicitly.  The solver's per-row scratch sits in a fixed 8 MiB device
+   array built into the library (held by every GPU that loads it until the
+   process exits), which limits a row to about 220 000 roots; larger rows are
+   rejected with CCF_ERR_INVALID_ARGUMENT.
+   start_roots: num_roots complex roots (device memory) at the branch centre.
+   ccs, errs, caustics: device arrays in the ccf_get_results layout of the
+   field; only the columns of steps 1..num_steps on this side are written
+   (caustics may be NULL).  stream: a cudaStream_t, or NULL for the default
+   stream; the call only enqueues work on it.  The first call on a device
+   looks up the scratch's device address; make that first call before any
+   stream capture.  All calls share the scratch and it keeps the last call's
+   contents: calls whose work overlaps on the GPU race and must be
+   serialised by the caller. */
+ccf_status ccf_continue_branch_noalloc(ccf_handle* h, int branch, int side, int num_steps, const double* start_roots,
+	double* ccs, double* errs, double* caustics, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
