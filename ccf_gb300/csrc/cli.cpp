@@ -211,7 +211,9 @@ int main(int argc, char* argv[])
 		}
 		catch (...)
 		{
-			std::string name = o.substr(o.find_first_not_of('-'));
+			/* the message names the long form of the option, as the reference's does */
+			size_t k = std::find(OPTS.begin(), OPTS.end(), o) - OPTS.begin();
+			std::string name = OPTS[k | 1].substr(2);
 			std::cerr << "Error. Invalid " << name << " input.\n";
 			return -1;
 		}

@@ -30,7 +30,7 @@ def test_help_and_argument_errors():
     rc, _, err = run("-s", "-0.5")
     assert rc == 255 and "smooth_fraction must be >= 0" in err
     rc, _, err = run("-pr", "fp16")
-    assert rc == 255 and "Invalid pr input" in err
+    assert rc == 255 and "Invalid precision input" in err
 
 
 @pytest.mark.gpu
