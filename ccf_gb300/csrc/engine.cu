@@ -237,11 +237,6 @@ ccf_status Engine::prepare_field(Field& f, int verbose)
 	if (p.write_mu_length_scales) CCF_TRY(f.mu.ensure(npts), "cudaMalloc(mu_length_scales)");
 	CCF_TRY(f.stats.ensure(16), "cudaMalloc(stats)");
 	CCF_TRY(cudaMemsetAsync(f.stats.ptr, 0, 16 * sizeof(unsigned long long), s), "memset");
-	if (p.precision == CCF_PRECISION_MIXED)
-	{
-		CCF_TRY(f.star_hilo.ensure(N), "cudaMalloc(star hilo)");
-		launch_star_hilo(s, N, f.star_pos.ptr, f.star_hilo.ptr);
-	}
 
 	/* info */
 	info.num_stars = N;
@@ -270,7 +265,7 @@ ccf_status Engine::prepare_field(Field& f, int verbose)
 	   per split level), FMM (upward per level, downward from level 2, leaf
 	   flags, scan, leaf records) */
 	const int lv = info.tree_levels;
-	info.kernel_launches = (d.star_input ? 0 : 1) + 1 + (p.precision == CCF_PRECISION_MIXED ? 1 : 0) + 1 + (lv + 1) + 4 * lv
+	info.kernel_launches = (d.star_input ? 0 : 1) + 1 + (p.precision == CCF_PRECISION_MIXED ? 2 : 0) + 1 + (lv + 1) + 4 * lv
 		+ (lv + 1) + std::max(0, lv - 1) + 3;
 	return CCF_OK;
 }
@@ -394,8 +389,24 @@ ccf_status Engine::build_fmm(Field& f)
 		f.leaf_center.ptr, f.leaf_inv_half.ptr, f.leaf_near_count.ptr, f.leaf_near.ptr, f.leaf_loc.ptr, f.leaf_loc3f.ptr,
 		f.node_leaf.ptr, f.level_out.ptr + 2);
 	CCF_TRY(cudaGetLastError(), "leaf_build_kernel");
+	if (p.precision == CCF_PRECISION_MIXED)
+	{
+		CCF_TRY(f.leaf_near_df.ensure((size_t)nl * MAX_NEAR), "cudaMalloc(leaves)");
+		CCF_TRY(f.leaf_mass_df.ensure((size_t)nl * MAX_NEAR), "cudaMalloc(leaves)");
+		CCF_TRY(f.leaf_loc_df.ensure((size_t)nl * 2 * (P + 1)), "cudaMalloc(leaves)");
+		CCF_TRY(f.leaf_ih_df.ensure(nl), "cudaMalloc(leaves)");
+		launch_leaf_df(s, nl, P, f.leaf_center.ptr, f.leaf_inv_half.ptr, f.leaf_near_count.ptr, f.leaf_near.ptr,
+			f.leaf_loc.ptr, f.leaf_near_df.ptr, f.leaf_mass_df.ptr, f.leaf_loc_df.ptr, f.leaf_ih_df.ptr);
+		CCF_TRY(cudaGetLastError(), "leaf_df_kernel");
+		/* split stars: poles of the Aberth sums and the off-field direct sums */
+		CCF_TRY(f.star_hilo.ensure(d.num_stars), "cudaMalloc(star hilo)");
+		CCF_TRY(f.star_mass_df.ensure(d.num_stars), "cudaMalloc(star hilo)");
+		launch_star_hilo(s, d.num_stars, f.star_pos.ptr, f.star_hilo.ptr, f.star_mass.ptr, f.star_mass_df.ptr);
+		CCF_TRY(cudaGetLastError(), "star_hilo_kernel");
+	}
 
 	/* smooth-mass polynomials */
+	float4 inv_corner_df = make_float4(0, 0, 0, 0);
 	SmoothPoly sp = smooth_polynomials(d.kappa_star, d.corner_x1, d.corner_x2, d.taylor_smooth);
 	{
 		std::vector<double2> d1(std::max(1, sp.m)), d2(std::max(1, sp.m)), a(sp.a.size());
@@ -407,6 +418,30 @@ ccf_status Engine::build_fmm(Field& f)
 			d2f[i] = make_float2((float)sp.d2[i].real(), (float)sp.d2[i].imag());
 		}
 		for (size_t i = 0; i < a.size(); i++) a[i] = make_double2(sp.a[i].real(), sp.a[i].imag());
+		/* double-float copies (hi = nearest float, lo = float of the remainder) */
+		auto split4 = [](std::complex<double> v) {
+			float rh = (float)v.real(), ih = (float)v.imag();
+			return make_float4(rh, ih, (float)(v.real() - (double)rh), (float)(v.imag() - (double)ih));
+		};
+		std::vector<float4> d1df(std::max(1, sp.m)), adf(sp.a.size());
+		for (int i = 0; i < sp.m; i++) d1df[i] = split4(sp.d1[i]);
+		/* alpha polynomial in w = zbar / c: B_n = A_n c^n.  |A_n| falls like
+		   |c|^(1-n) and leaves the FP32 range for large fields, B_n stays O(|c|) */
+		{
+			std::complex<long double> cn(1.0L, 0.0L);
+			const std::complex<long double> cl((long double)d.corner_x1, (long double)d.corner_x2);
+			for (size_t i = 0; i < sp.a.size(); i++)
+			{
+				const std::complex<long double> b = std::complex<long double>(sp.a[i].real(), sp.a[i].imag()) * cn;
+				adf[i] = split4(std::complex<double>((double)b.real(), (double)b.imag()));
+				cn *= cl;
+			}
+		}
+		inv_corner_df = split4(sp.inv_corner);
+		CCF_TRY(f.sm_d1_df.ensure(d1df.size()), "cudaMalloc(smooth)");
+		CCF_TRY(f.sm_a_df.ensure(adf.size()), "cudaMalloc(smooth)");
+		CCF_TRY(cudaMemcpyAsync(f.sm_d1_df.ptr, d1df.data(), d1df.size() * sizeof(float4), cudaMemcpyHostToDevice, s), "smooth");
+		CCF_TRY(cudaMemcpyAsync(f.sm_a_df.ptr, adf.data(), adf.size() * sizeof(float4), cudaMemcpyHostToDevice, s), "smooth");
 		CCF_TRY(f.sm_d1.ensure(d1.size()), "cudaMalloc(smooth)");
 		CCF_TRY(f.sm_d2.ensure(d2.size()), "cudaMalloc(smooth)");
 		CCF_TRY(f.sm_d2f.ensure(d2f.size()), "cudaMalloc(smooth)");
@@ -459,6 +494,15 @@ ccf_status Engine::build_fmm(Field& f)
 	V.leaf_near = f.leaf_near.ptr;
 	V.leaf_loc = f.leaf_loc.ptr;
 	V.leaf_loc3f = f.leaf_loc3f.ptr;
+	V.leaf_near_df = f.leaf_near_df.ptr;
+	V.leaf_mass_df = f.leaf_mass_df.ptr;
+	V.leaf_loc_df = f.leaf_loc_df.ptr;
+	V.leaf_ih_df = f.leaf_ih_df.ptr;
+	V.smooth_d1_df = f.sm_d1_df.ptr;
+	V.smooth_a_df = f.sm_a_df.ptr;
+	V.inv_corner_df = inv_corner_df;
+	V.star_df = f.star_hilo.ptr;
+	V.star_mass_df = f.star_mass_df.ptr;
 	CCF_TRY(f.view_dev.ensure(1), "cudaMalloc(view)");
 	CCF_TRY(cudaMemcpyAsync(f.view_dev.ptr, &V, sizeof(V), cudaMemcpyHostToDevice, s), "view");
 	return CCF_OK;

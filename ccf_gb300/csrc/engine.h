@@ -80,6 +80,7 @@ struct Field
 	DBuf<double2> star_pos, star_tmp_pos;
 	DBuf<double> star_mass, star_tmp_mass;
 	DBuf<float4> star_hilo;
+	DBuf<float2> star_mass_df;
 	DBuf<double> stats5;
 
 	/* tree */
@@ -101,11 +102,14 @@ struct Field
 	DBuf<NearStar> leaf_near;
 	DBuf<double2> leaf_loc;
 	DBuf<float2> leaf_loc3f;
+	DBuf<float4> leaf_near_df, leaf_loc_df;
+	DBuf<float2> leaf_mass_df, leaf_ih_df;
 	int num_leaves = 0;
 
 	/* smooth-mass polynomials */
 	DBuf<double2> sm_d1, sm_d2, sm_a;
 	DBuf<float2> sm_d2f;
+	DBuf<float4> sm_d1_df, sm_a_df;
 
 	/* device view */
 	FieldView view;

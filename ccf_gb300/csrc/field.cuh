@@ -76,6 +76,17 @@ struct FieldView
 	const NearStar* leaf_near;   /* [leaf * MAX_NEAR + i] */
 	const double2* leaf_loc;     /* [(leaf * 3 + k) * (P + 1) + i], k = 0: alpha, 1: d/dzbar, 2: d2/dzbar2 */
 	const float2* leaf_loc3f;    /* FP32 copy of the k = 2 block, [leaf * (P + 1) + i] */
+
+	/* double-float copies for the mixed-precision evaluators (field_df.cuh) */
+	const float4* leaf_near_df;  /* [leaf * MAX_NEAR + i] (z_i - leaf centre), complex double-float */
+	const float2* leaf_mass_df;  /* [leaf * MAX_NEAR + i] */
+	const float4* leaf_loc_df;   /* [(leaf * 2 + k) * (P + 1) + i], k = 0: alpha, 1: d/dzbar */
+	const float2* leaf_ih_df;    /* [leaf] 1/h */
+	const float4* smooth_d1_df;  /* [smooth_m] */
+	const float4* smooth_a_df;   /* [taylor_smooth + 2] A_n c^n: the alpha polynomial in zbar / c */
+	float4 inv_corner_df;
+	const float4* star_df;       /* [num_stars] star positions, split (x_hi, y_hi, x_lo, y_lo) */
+	const float2* star_mass_df;  /* [num_stars] */
 };
 
 /* leaf containing z, or -1 when z lies outside the root box (the reference
@@ -365,9 +376,22 @@ CCF_D void eval_f64(const FieldView& F, int leaf, double2 z, double cphi, double
 	}
 }
 
+/* The reduced-precision smooth-mass polynomials (the FP32 f' below, the
+   double-float ones of field_df.cuh) are used only inside the circle through
+   the field's corners, |z / c|^2 < SMOOTH_DF_RANGE.  There the Taylor series
+   converges and its terms are below ~1, so double-float rounding is ~1e-15.
+   Outside, the terms grow like |z / c|^(2m) and cancel; the FP64 forms keep
+   that cancellation at the reference's own FP64 rounding, and no FP32 part
+   can overflow. */
+constexpr double SMOOTH_DF_RANGE = 1.0;
+CCF_D bool smooth_df_ok(const FieldView& F, double2 z)
+{
+	return z.x * z.x + z.y * z.y < SMOOTH_DF_RANGE * F.corner_abs * F.corner_abs;
+}
+
 /* f'(z) in FP32 for the mixed-precision solver: only the step size depends
-   on it, never the converged root.  Off-field points use the FP64 s3 of the
-   warp-cooperative sum. */
+   on it, never the converged root.  Off-field points take s3_off, the direct
+   sum over every star. */
 CCF_D float2 eval_df32(const FieldView& F, int leaf, double2 z, double2 s3_off)
 {
 	float2 s3 = make_float2(0, 0);
@@ -400,7 +424,7 @@ CCF_D float2 eval_df32(const FieldView& F, int leaf, double2 z, double2 s3_off)
 		s3 = make_float2((float)s3_off.x, (float)s3_off.y);
 	}
 	float2 d2s;
-	if (F.rectangular && F.approx && F.smooth_m > 0)
+	if (F.rectangular && F.approx && F.smooth_m > 0 && smooth_df_ok(F, z))
 	{
 		double2 zb = cconj(z);
 		double2 rd = cmul(zb, F.inv_corner);

@@ -1,0 +1,222 @@
+/******************************************************************************
+field_df.cuh -- the critical-curve function and the epilogue quantities in
+double-float arithmetic, for the mixed-precision solver.
+
+Same formulas as field.cuh (reference: include/alpha_star.cuh,
+alpha_local.cuh, alpha_smooth.cuh, ccf_functions.cuh:33-121, :419-467), on
+the FP32 pipe.  Coordinates are taken relative to the leaf centre before they
+are split into double-float (the leaf-relative positions of the near stars are
+formed in FP64 and stored split), so a difference z - z_i keeps ~1e-14 of the
+leaf size; f comes out with an absolute error of ~1e-13 for ordinary roots,
+four orders of magnitude below what moves a root by 1e-9 theta_star.  The
+final assembly of f and of the caustic is done in FP64 from the
+double-float partial results.  Off-field points (outside the root box) go
+through the same evaluators with the direct star sums (star_term_df, summed
+by the whole CTA in solver.cu) in place of the leaf's near sums and local
+expansion.
+******************************************************************************/
+#pragma once
+
+#include "dfloat.cuh"
+#include "field.cuh"
+
+namespace ccf
+{
+
+struct SumsDF
+{
+	dfc s1, s2;
+};
+
+/* s1 = sum m / d, s2 = sum m / d^2 over the leaf's near stars, d = z - z_i */
+template <bool NEED1>
+CCF_D SumsDF leaf_sums_df(const FieldView& F, int leaf, double2 z)
+{
+	const double2 c = F.leaf_center[leaf];
+	const dfc zr = dfc_from(make_double2(z.x - c.x, z.y - c.y));
+	SumsDF a;
+	a.s1 = {{0.f, 0.f}, {0.f, 0.f}};
+	a.s2 = a.s1;
+	const int n = F.leaf_near_count[leaf];
+	const float4* P = F.leaf_near_df + (size_t)leaf * MAX_NEAR;
+	const float2* M = F.leaf_mass_df + (size_t)leaf * MAX_NEAR;
+	for (int i = 0; i < n; i++)
+	{
+		const dfc s = dfc_load(P[i]);
+		const float2 mm = M[i];
+		const dfl m = {mm.x, mm.y};
+		const dfl dx = df_sub(zr.re, s.re);
+		const dfl dy = df_sub(zr.im, s.im);
+		const dfl r = df_rcp(df_add_fast(df_sqr(dx), df_sqr(dy)));
+		const dfl ix = df_mul(dx, r);
+		const dfl iy = df_neg(df_mul(dy, r));                     /* 1/d */
+		const dfl i2x = df_add(df_sqr(ix), df_neg(df_sqr(iy)));
+		dfl i2y = df_mul(ix, iy);
+		i2y = {2.f * i2y.hi, 2.f * i2y.lo};                        /* 1/d^2 */
+		a.s2.re = df_add_fast(a.s2.re, df_mul(m, i2x));
+		a.s2.im = df_add_fast(a.s2.im, df_mul(m, i2y));
+		if (NEED1)
+		{
+			a.s1.re = df_add_fast(a.s1.re, df_mul(m, ix));
+			a.s1.im = df_add_fast(a.s1.im, df_mul(m, iy));
+		}
+	}
+	return a;
+}
+
+/* One star's terms at an off-field point z (absolute coordinates, double-
+   float): d = z - z_i from the split star position p = (x_hi, y_hi, x_lo,
+   y_lo) and split mass mm; adds m/d^2 to s2, m/d to s1 (NEED1) and m/d^3 to
+   s3 in double-float (S3DF) or in FP32 to s3f.  Off-field points are at least
+   the gap between the star field and the root box away from every star, so
+   the ~2^-48 |z| resolution of the split coordinates is a relative error of
+   ~1e-14 in each term. */
+template <bool NEED1, bool S3DF>
+CCF_D void star_term_df(SumsDF& a, dfc& s3, float2& s3f, const dfc& z, float4 p, float2 mm)
+{
+	const dfc s = dfc_load(p);
+	const dfl m = {mm.x, mm.y};
+	const dfl dx = df_sub(z.re, s.re);
+	const dfl dy = df_sub(z.im, s.im);
+	const dfl r = df_rcp(df_add_fast(df_sqr(dx), df_sqr(dy)));
+	const dfl ix = df_mul(dx, r);
+	const dfl iy = df_neg(df_mul(dy, r));                     /* 1/d */
+	const dfl i2x = df_add(df_sqr(ix), df_neg(df_sqr(iy)));
+	dfl i2y = df_mul(ix, iy);
+	i2y = {2.f * i2y.hi, 2.f * i2y.lo};                        /* 1/d^2 */
+	a.s2.re = df_add_fast(a.s2.re, df_mul(m, i2x));
+	a.s2.im = df_add_fast(a.s2.im, df_mul(m, i2y));
+	if (NEED1)
+	{
+		a.s1.re = df_add_fast(a.s1.re, df_mul(m, ix));
+		a.s1.im = df_add_fast(a.s1.im, df_mul(m, iy));
+	}
+	if (S3DF)
+	{
+		const dfl i3x = df_add(df_mul(i2x, ix), df_neg(df_mul(i2y, iy)));
+		const dfl i3y = df_add(df_mul(i2x, iy), df_mul(i2y, ix));   /* 1/d^3 */
+		s3.re = df_add_fast(s3.re, df_mul(m, i3x));
+		s3.im = df_add_fast(s3.im, df_mul(m, i3y));
+	}
+	else
+	{
+		const float i3x = i2x.hi * ix.hi - i2y.hi * iy.hi;
+		const float i3y = i2x.hi * iy.hi + i2y.hi * ix.hi;
+		s3f.x = fmaf(m.hi, i3x, s3f.x);
+		s3f.y = fmaf(m.hi, i3y, s3f.y);
+	}
+}
+
+/* Horner of a double-float coefficient block: sum_{i >= first} L[i] dz^(i - first) */
+CCF_D dfc horner_df(const float4* L, int P, int first, dfc dz)
+{
+	dfc acc = dfc_load(L[P]);
+	for (int i = P - 1; i >= first; i--) acc = dfc_add(dfc_mul(acc, dz), dfc_load(L[i]));
+	return acc;
+}
+
+CCF_D dfc leaf_dz_df(const FieldView& F, int leaf, double2 z)
+{
+	const double2 c = F.leaf_center[leaf];
+	const dfc zr = dfc_from(make_double2(z.x - c.x, z.y - c.y));
+	const float2 ihf = F.leaf_ih_df[leaf];
+	const dfl ih = {ihf.x, ihf.y};
+	return {df_mul(zr.re, ih), df_mul(zr.im, ih)};
+}
+
+/* d alpha_smooth / d zbar for the rectangular Taylor form, double-float */
+CCF_D double2 smooth_dzbar_df(const FieldView& F, double2 z)
+{
+	if (F.smooth_m <= 0) return make_double2(F.smooth_k1, 0);
+	const dfc zb = dfc_from(make_double2(z.x, -z.y));
+	const dfc r = dfc_mul(zb, dfc_load(F.inv_corner_df));
+	const dfc u = dfc_mul(r, r);
+	dfc acc = dfc_load(F.smooth_d1_df[F.smooth_m - 1]);
+	for (int m = F.smooth_m - 2; m >= 0; m--) acc = dfc_add(dfc_mul(acc, u), dfc_load(F.smooth_d1_df[m]));
+	acc = dfc_mul(acc, u);
+	double2 d = dfc_to(acc);
+	d.x += F.smooth_k1;
+	return d;
+}
+
+/* alpha_smooth for the rectangular Taylor form, double-float polynomial in
+   w = zbar / c with the coefficients A_n c^n (the same polynomial as
+   smooth_alpha's sum A_n zbar^n, whose coefficients underflow FP32) */
+CCF_D double2 smooth_alpha_df(const FieldView& F, double2 z)
+{
+	const double k = F.kappa_star;
+	const dfc w = dfc_mul(dfc_from(make_double2(z.x, -z.y)), dfc_load(F.inv_corner_df));
+	const int n = F.taylor_smooth + 1;
+	dfc acc = dfc_load(F.smooth_a_df[n]);
+	for (int i = n - 1; i >= 0; i--) acc = dfc_add(dfc_mul(acc, w), dfc_load(F.smooth_a_df[i]));
+	double2 a = cmul(dfc_to(acc), make_double2(0, -k / PI));
+	a.x -= k * 2 * (F.corner.x + z.x);
+	return a;
+}
+
+CCF_D double2 smooth_dzbar_any(const FieldView& F, double2 z)
+{
+	if (F.rectangular && F.approx && smooth_df_ok(F, z)) return smooth_dzbar_df(F, z);
+	return smooth_dzbar(F, z);
+}
+CCF_D double2 smooth_alpha_any(const FieldView& F, double2 z)
+{
+	if (F.rectangular && F.approx && smooth_df_ok(F, z)) return smooth_alpha_df(F, z);
+	return smooth_alpha(F, z);
+}
+
+/* f(z; phi) in double-float.  Inside the root box (leaf >= 0) the star terms
+   are the leaf's near sums and local expansion; a point outside it (leaf < 0)
+   takes the direct sums over every star from ext (the reference's direct sum
+   there, include/tree_node.cuh:535-539), so both go through the same code. */
+CCF_D double2 eval_f_df(const FieldView& F, int leaf, double2 z, double cphi, double sphi, const NearSums& ext)
+{
+	double2 s2 = ext.s2, dl = make_double2(0, 0);
+	if (leaf >= 0)
+	{
+		const SumsDF S = leaf_sums_df<false>(F, leaf, z);
+		const int P = F.order;
+		const dfc dz = leaf_dz_df(F, leaf, z);
+		dl = dfc_to(horner_df(F.leaf_loc_df + ((size_t)leaf * 2 + 1) * (P + 1), P, 2, dz));
+		s2 = dfc_to(S.s2);
+	}
+	const double2 ds = smooth_dzbar_any(F, z);
+	const double a = 1 - F.kappa_tot - smooth_dz(F, z);
+	double2 f;
+	f.x = F.shear + F.theta2 * s2.x - dl.x - ds.x - a * cphi;
+	f.y = F.theta2 * s2.y - dl.y + ds.y + a * sphi;
+	return f;
+}
+
+/* 1/mu bound and caustic of a final point, double-float; star terms as in
+   eval_f_df (leaf sums and local expansion, or ext off the root box) */
+CCF_D PointResult eval_point_df(const FieldView& F, int leaf, double2 z, double cphi, double sphi, const NearSums& ext)
+{
+	double2 s1 = ext.s1, s2 = ext.s2, al = make_double2(0, 0), dl = make_double2(0, 0);
+	if (leaf >= 0)
+	{
+		const SumsDF S = leaf_sums_df<true>(F, leaf, z);
+		const int P = F.order;
+		const dfc dz = leaf_dz_df(F, leaf, z);
+		const float4* L = F.leaf_loc_df + (size_t)leaf * 2 * (P + 1);
+		al = dfc_to(horner_df(L, P, 1, dz));
+		dl = dfc_to(horner_df(L + (P + 1), P, 2, dz));
+		s1 = dfc_to(S.s1);
+		s2 = dfc_to(S.s2);
+	}
+	const double2 ds = smooth_dzbar_any(F, z);
+	const double a = 1 - F.kappa_tot - smooth_dz(F, z);
+	double2 f;
+	f.x = F.shear + F.theta2 * s2.x - dl.x - ds.x - a * cphi;
+	f.y = F.theta2 * s2.y - dl.y + ds.y + a * sphi;
+	const double af = hypot(f.x, f.y);
+	PointResult out;
+	out.err = fmax(fabs(af * (af + 2 * a)), fabs(af * (af - 2 * a)));
+	const double2 as = smooth_alpha_any(F, z);
+	out.w.x = (1 - F.kappa_tot) * z.x + F.shear * z.x - F.theta2 * s1.x - al.x - as.x;
+	out.w.y = (1 - F.kappa_tot) * z.y - F.shear * z.y + F.theta2 * s1.y + al.y - as.y;
+	out.mu_length = 0;
+	return out;
+}
+
+} /* namespace ccf */

@@ -279,3 +279,53 @@ void launch_leaf_build(cudaStream_t s, const TreeDev& T, int num_nodes, const in
 }
 
 } /* namespace ccf */
+
+namespace ccf
+{
+
+/* double-float copies of the leaf records for the mixed-precision evaluators:
+   near stars relative to the leaf centre (formed in FP64, then split),
+   masses, the alpha and d/dzbar coefficient blocks, and 1/h.  One warp per
+   leaf. */
+__global__ void leaf_df_kernel(int num_leaves, int P, const double2* __restrict__ leaf_center,
+	const double* __restrict__ leaf_inv_half, const int* __restrict__ near_count, const NearStar* __restrict__ near,
+	const double2* __restrict__ loc, float4* __restrict__ near_df, float2* __restrict__ mass_df, float4* __restrict__ loc_df,
+	float2* __restrict__ ih_df)
+{
+	const int l = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+	const int i = threadIdx.x & 31;
+	if (l >= num_leaves) return;
+	const double2 c = leaf_center[l];
+	auto split = [](double x) {
+		float h = __double2float_rn(x);
+		return make_float2(h, __double2float_rn(x - (double)h));
+	};
+	if (i < near_count[l])
+	{
+		NearStar s = near[(size_t)l * MAX_NEAR + i];
+		float2 x = split(s.x - c.x), y = split(s.y - c.y);
+		near_df[(size_t)l * MAX_NEAR + i] = make_float4(x.x, y.x, x.y, y.y);
+		mass_df[(size_t)l * MAX_NEAR + i] = split(s.m);
+	}
+	if (i <= P)
+	{
+		for (int k = 0; k < 2; k++)
+		{
+			double2 v = loc[((size_t)l * 3 + k) * (P + 1) + i];
+			float2 re = split(v.x), im = split(v.y);
+			loc_df[((size_t)l * 2 + k) * (P + 1) + i] = make_float4(re.x, im.x, re.y, im.y);
+		}
+	}
+	if (i == 0) ih_df[l] = split(leaf_inv_half[l]);
+}
+
+void launch_leaf_df(cudaStream_t s, int num_leaves, int P, const double2* leaf_center, const double* leaf_inv_half,
+	const int* near_count, const NearStar* near, const double2* loc, float4* near_df, float2* mass_df, float4* loc_df,
+	float2* ih_df)
+{
+	const int warps = 4;
+	leaf_df_kernel<<<(num_leaves + warps - 1) / warps, warps * 32, 0, s>>>(num_leaves, P, leaf_center, leaf_inv_half,
+		near_count, near, loc, near_df, mass_df, loc_df, ih_df);
+}
+
+} /* namespace ccf */

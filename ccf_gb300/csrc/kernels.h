@@ -96,7 +96,8 @@ void launch_generate_stars(cudaStream_t s, int n, int seed, int rectangular, dou
 void launch_star_stats(cudaStream_t s, int n, const double* mass, double* out);
 void launch_seed_roots(cudaStream_t s, int nstars, int nroots, int nrows, const double2* pos, double corner_abs,
 	double2* master, float4* snap32, double2* snap64);
-void launch_star_hilo(cudaStream_t s, int n, const double2* pos, float4* out);
+void launch_star_hilo(cudaStream_t s, int n, const double2* pos, float4* out, const double* mass = nullptr,
+	float2* mass_out = nullptr);
 
 /* tree.cu */
 void launch_tree_root(cudaStream_t s, const TreeDev& T, double half, int nstars);
@@ -116,6 +117,10 @@ void launch_fmm_downward(cudaStream_t s, const TreeDev& T, int start, int count,
 void launch_leaf_build(cudaStream_t s, const TreeDev& T, int num_nodes, const int* leaf_index, int P, double theta2,
 	const double2* pos, const double* mass, const double2* local, double2* leaf_center, double* leaf_inv_half,
 	int* leaf_near_count, NearStar* leaf_near, double2* leaf_loc, float2* leaf_loc3f, int* node_leaf, int* err);
+
+void launch_leaf_df(cudaStream_t s, int num_leaves, int P, const double2* leaf_center, const double* leaf_inv_half,
+	const int* near_count, const NearStar* near, const double2* loc, float4* near_df, float2* mass_df, float4* loc_df,
+	float2* ih_df);
 
 /* solver.cu */
 int solver_blocks_per_sm(bool mixed);

@@ -23,8 +23,10 @@ GB300 design:
   * mixed precision: the correction sums run in FP32 on the split hi + lo
     form of the coordinates (differences keep their relative accuracy for
     nearby roots), per-chunk partial sums are accumulated in FP64; the
-    critical-curve function f is always FP64, so the converged roots are
-    those of the FP64 function: the sums and f' only set the step size;
+    critical-curve function f is evaluated in double-float (two FP32 numbers,
+    ~48 significant bits, field_df.cuh) on the FP32 pipe, which GB300 runs 62
+    times faster than its FP64 pipe; f' is FP32.  The converged roots are the
+    zeros of f to ~1e-13: the sums and f' only set the step size;
   * a root is final once its step is below 1e-9 theta_star (the reference's
     test, ccf_functions.cuh:385); sweeps stop when no root of the row is
     active or the sweep cap is reached;
@@ -32,6 +34,7 @@ GB300 design:
     each point are computed in the epilogue of its phi step and written
     straight into the output layout, so no transpose pass is needed.
 ******************************************************************************/
+#include "field_df.cuh"
 #include "kernels.h"
 
 #include <cooperative_groups.h>
@@ -61,6 +64,87 @@ struct Src
 	using T = typename std::conditional<MIXED, float4, double2>::type;
 };
 
+constexpr int OFF_CAP = 64;      /* off-field points summed by the CTA per pass */
+
+/* Star sums of the off-field points pts[0..K), K <= OFF_CAP.  A point outside
+   the root box takes the direct sum over every star, as in the reference
+   (include/tree_node.cuh:535-539, include/alpha_star.cuh:26-37).  The whole
+   CTA works on each point: every thread takes every NT-th star, the warps
+   reduce by shuffles and the per-warp partials meet in shared memory (red,
+   K * NT/32 * 6 doubles).  MIXED evaluates in double-float on the FP32 pipe
+   from the split star arrays, s3 in double-float only when S3DF; otherwise
+   FP64.  All threads of the CTA must call it; it ends with a barrier, after
+   which out[0..K) holds the sums. */
+template <bool MIXED, bool NEED1, bool S3DF>
+__device__ void offfield_sums_cta(const FieldView& F, const double2* pts, int K, NearSums* out, double* red)
+{
+	const unsigned full = 0xffffffffu;
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	for (int k = 0; k < K; k++)
+	{
+		double v[6];
+		if constexpr (MIXED)
+		{
+			const dfc z = dfc_from(pts[k]);
+			SumsDF a;
+			a.s1 = {{0.f, 0.f}, {0.f, 0.f}};
+			a.s2 = a.s1;
+			dfc s3 = a.s1;
+			float2 s3f = make_float2(0.f, 0.f);
+			for (int i = threadIdx.x; i < F.num_stars; i += NT)
+				star_term_df<NEED1, S3DF>(a, s3, s3f, z, F.star_df[i], F.star_mass_df[i]);
+			if (!S3DF) s3 = {{s3f.x, 0.f}, {s3f.y, 0.f}};
+			dfl w[6] = {a.s1.re, a.s1.im, a.s2.re, a.s2.im, s3.re, s3.im};
+#pragma unroll
+			for (int c = 0; c < 6; c++)
+			{
+				for (int o = 16; o > 0; o >>= 1)
+				{
+					dfl u = {__shfl_xor_sync(full, w[c].hi, o), __shfl_xor_sync(full, w[c].lo, o)};
+					w[c] = df_add(w[c], u);
+				}
+				v[c] = df_to_double(w[c]);
+			}
+		}
+		else
+		{
+			NearSums a = zero_sums();
+			for (int i = threadIdx.x; i < F.num_stars; i += NT)
+			{
+				const double2 p = F.star_pos[i];
+				star_term<NEED1, true>(a, pts[k], p.x, p.y, F.star_mass[i]);
+			}
+			double u[6] = {a.s1.x, a.s1.y, a.s2.x, a.s2.y, a.s3.x, a.s3.y};
+#pragma unroll
+			for (int c = 0; c < 6; c++)
+			{
+				for (int o = 16; o > 0; o >>= 1) u[c] += __shfl_xor_sync(full, u[c], o);
+				v[c] = u[c];
+			}
+		}
+		if (lane == 0)
+		{
+#pragma unroll
+			for (int c = 0; c < 6; c++) red[(k * (NT / 32) + warp) * 6 + c] = v[c];
+		}
+	}
+	__syncthreads();
+	if (threadIdx.x < K)
+	{
+		const int k = threadIdx.x;
+		double v[6] = {0, 0, 0, 0, 0, 0};
+		for (int q = 0; q < NT / 32; q++)
+		{
+#pragma unroll
+			for (int c = 0; c < 6; c++) v[c] += red[(k * (NT / 32) + q) * 6 + c];
+		}
+		out[k].s1 = make_double2(v[0], v[1]);
+		out[k].s2 = make_double2(v[2], v[3]);
+		out[k].s3 = make_double2(v[4], v[5]);
+	}
+	__syncthreads();
+}
+
 /* phase of step j of a row (include/ccf_functions.cuh:338-344) */
 CCF_D double row_phi(int c, int nb, int nphi, int side, int j)
 {
@@ -70,20 +154,20 @@ CCF_D double row_phi(int c, int nb, int nphi, int side, int j)
 }
 
 /* One Aberth step for the target of every lane with valid set, given its
-   correction sum S; returns 0, 1 when the root became final, 2 when the step
-   was not finite (the root is then frozen).  All 32 lanes of the warp must
-   call it: off-field targets take their star sums from the whole warp.  Not
-   inlined: the FP64 evaluation needs its registers once, not once per
-   unrolled target. */
+   leaf and its correction sum S; returns 0, 1 when the root became final, 2
+   when the step was not finite (the root is then frozen).  An off-field
+   target (leaf < 0) takes its star sums from off when have_off is set (the
+   CTA computed them) and otherwise from the whole warp -- so all 32 lanes of
+   the warp must call it.  Not inlined: the evaluation needs its registers
+   once, not once per unrolled target. */
 template <bool MIXED>
 __device__ __noinline__ int aberth_update_warp(const FieldView& F, double2* __restrict__ master, unsigned char* __restrict__ fin,
-	bool valid, int a, double2 S, bool disc_exact, double cphi, double sphi)
+	bool valid, int a, int leaf, bool have_off, NearSums off, double2 S, bool disc_exact, double cphi, double sphi)
 {
 	double2 z = valid ? master[a] : make_double2(0, 0);
-	int leaf = valid ? find_leaf(F, z) : 0;
-	NearSums ns = zero_sums();
-	if (valid && leaf >= 0) ns = leaf_sums<false, !MIXED>(F, leaf, z);
-	offfield_sums_warp<false, true>(F, valid && leaf < 0, z, ns);
+	NearSums ns = have_off ? off : zero_sums();
+	if (!MIXED && valid && leaf >= 0) ns = leaf_sums<false, true>(F, leaf, z);
+	offfield_sums_warp<false, true>(F, valid && leaf < 0 && !have_off, z, ns);
 	if (!valid) return 0;
 	if (disc_exact)
 	{
@@ -94,7 +178,8 @@ __device__ __noinline__ int aberth_update_warp(const FieldView& F, double2* __re
 	double2 f, df;
 	if constexpr (MIXED)
 	{
-		eval_f64<false>(F, leaf, z, cphi, sphi, ns, f, df);
+		/* f in double-float on the FP32 pipe, off-field points included */
+		f = eval_f_df(F, leaf, z, cphi, sphi, ns);
 		float2 d32 = eval_df32(F, leaf, z, ns.s3);
 		df = make_double2(d32.x, d32.y);
 	}
@@ -120,18 +205,23 @@ __device__ __noinline__ int aberth_update_warp(const FieldView& F, double2* __re
 }
 
 /* outputs of one final root per lane: position, 1/mu bound, caustic,
-   length scale.  All 32 lanes must call it (see aberth_update_warp). */
-__device__ __noinline__ void point_epilogue_warp(const FieldView& F, const FieldOut& O, bool valid, double2 z, size_t out,
-	double cphi, double sphi, double* maxerr, int* nan)
+   length scale; returns false when the 1/mu bound is not finite.  All 32
+   lanes must call it (see aberth_update_warp for leaf, have_off and off).
+   With DF and no length scales every point is evaluated in double-float (off
+   the root box from the star sums); length scales use FP64. */
+template <bool DF>
+__device__ __noinline__ bool point_epilogue_warp(const FieldView& F, const FieldOut& O, bool valid, double2 z, int leaf,
+	bool have_off, NearSums off, size_t out, double cphi, double sphi, double* maxerr)
 {
-	int leaf = valid ? find_leaf(F, z) : 0;
-	NearSums ns = zero_sums();
+	NearSums ns = have_off ? off : zero_sums();
 	const bool mu = O.mu != nullptr;
-	if (valid && leaf >= 0) ns = mu ? leaf_sums<true, true>(F, leaf, z) : leaf_sums<true, false>(F, leaf, z);
-	offfield_sums_warp<true, true>(F, valid && leaf < 0, z, ns);
-	if (!valid) return;
+	const bool use_df = DF && !mu;
+	if (!use_df && valid && leaf >= 0) ns = mu ? leaf_sums<true, true>(F, leaf, z) : leaf_sums<true, false>(F, leaf, z);
+	offfield_sums_warp<true, true>(F, valid && leaf < 0 && !have_off, z, ns);
+	if (!valid) return true;
 	PointResult pr;
-	if (O.caustics && mu) pr = eval_point<true, true>(F, leaf, z, cphi, sphi, ns);
+	if (use_df) pr = eval_point_df(F, leaf, z, cphi, sphi, ns);
+	else if (O.caustics && mu) pr = eval_point<true, true>(F, leaf, z, cphi, sphi, ns);
 	else if (O.caustics) pr = eval_point<true, false>(F, leaf, z, cphi, sphi, ns);
 	else if (mu) pr = eval_point<false, true>(F, leaf, z, cphi, sphi, ns);
 	else pr = eval_point<false, false>(F, leaf, z, cphi, sphi, ns);
@@ -139,8 +229,9 @@ __device__ __noinline__ void point_epilogue_warp(const FieldView& F, const Field
 	O.errs[out] = pr.err;
 	if (O.caustics) O.caustics[out] = pr.w;
 	if (mu) O.mu[out] = pr.mu_length;
-	if (isfinite(pr.err)) atomicMax((unsigned long long*)maxerr, (unsigned long long)__double_as_longlong(pr.err));
-	else atomicOr(nan, 1);
+	if (!isfinite(pr.err)) return false;
+	atomicMax((unsigned long long*)maxerr, (unsigned long long)__double_as_longlong(pr.err));
+	return true;
 }
 
 template <bool MIXED>
@@ -161,8 +252,13 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 	__shared__ int s_pre[9];
 	__shared__ unsigned long long s_upd, s_terms, s_unconv;
 	__shared__ double s_maxerr;
-	__shared__ int s_nan;
+	__shared__ int s_nan_err, s_nan_step;   /* set by plain stores: every writer stores 1 */
+	__shared__ int s_noff;
+	__shared__ double2 s_offz[OFF_CAP];
+	__shared__ NearSums s_offs[OFF_CAP];
 	__shared__ __align__(16) SrcT sbuf[2][CHUNK];
+	static_assert(OFF_CAP * (NT / 32) * 6 * sizeof(double) <= sizeof(sbuf), "off-field scratch");
+	double* const red_off = reinterpret_cast<double*>(&sbuf[0][0]);
 
 	if (threadIdx.x == 0)
 	{
@@ -173,7 +269,8 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 		s_terms = 0;
 		s_unconv = 0;
 		s_maxerr = 0;
-		s_nan = 0;
+		s_nan_err = 0;
+		s_nan_step = 0;
 	}
 	__syncthreads();
 	const FieldView& F = sF;
@@ -251,9 +348,24 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 			const int total = s_pre[csize];
 			if (total == 0 || it >= max_it) break;
 
-			const int ntiles = (total + TILE - 1) / TILE;
+			/* Source split S: when the sweep has fewer full tiles than the
+			   cluster has CTAs, a tile shrinks to TILE / S targets and the S warps
+			   of each 64-target group split every source chunk between them; the
+			   partial sums meet in shared memory.  Tail sweeps with a handful of
+			   active roots then cost 1/S of a full tile on every CTA instead of a
+			   full tile on one CTA. */
+			int S = 1;
+			while (S < NT / 32 && (total + TILE / S - 1) / (TILE / S) < csize) S *= 2;
+			const int TT = TILE / S;
+			const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+			const int part = warp % S;
+			const int group = warp / S;
+			const int ntiles = (total + TT - 1) / TT;
 			for (int tile = crank; tile < ntiles; tile += csize)
 			{
+				/* the barriers of the chunk loop order this reset before any
+				   target of the tile is counted */
+				if (threadIdx.x == 0) s_noff = 0;
 				int tid_a[TPT];
 				bool valid[TPT];
 				SrcT zs[TPT];
@@ -261,7 +373,7 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 #pragma unroll
 				for (int t = 0; t < TPT; t++)
 				{
-					int g = tile * TILE + t * NT + threadIdx.x;
+					int g = tile * TT + group * 64 + t * 32 + lane;
 					valid[t] = g < total;
 					int a = 0;
 					if (valid[t])
@@ -303,6 +415,7 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 					cp_async_wait<1>();
 					__syncthreads();
 					const int n = ch < nrc ? min(CHUNK, R - ch * CHUNK) : min(CHUNK, N - (ch - nrc) * CHUNK);
+					const int j0 = (n * part) / S, j1 = (n * (part + 1)) / S;
 					const SrcT* sb = sbuf[ch & 1];
 					if constexpr (MIXED)
 					{
@@ -310,7 +423,7 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 #pragma unroll
 						for (int t = 0; t < TPT; t++) { ax[t] = 0.f; ay[t] = 0.f; }
 #pragma unroll 4
-						for (int jj = 0; jj < n; jj++)
+						for (int jj = j0; jj < j1; jj++)
 						{
 							float4 s = sb[jj];
 #pragma unroll
@@ -338,7 +451,7 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 #pragma unroll
 						for (int t = 0; t < TPT; t++) { ax[t] = 0; ay[t] = 0; }
 #pragma unroll 2
-						for (int jj = 0; jj < n; jj++)
+						for (int jj = j0; jj < j1; jj++)
 						{
 							double2 s = sb[jj];
 #pragma unroll
@@ -362,20 +475,81 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 					}
 					__syncthreads();
 				}
+				if (S > 1)
+				{
+					/* combine the S partial sums of each target (the staging
+					   buffer is free: the last chunk ended with a barrier) */
+					double2* red = reinterpret_cast<double2*>(&sbuf[0][0]);
+#pragma unroll
+					for (int t = 0; t < TPT; t++)
+					{
+						int slot = (part * (NT / 32 / S) + group) * 64 + t * 32 + lane;
+						red[2 * slot] = totR[t];
+						red[2 * slot + 1] = totS[t];
+					}
+					__syncthreads();
+					if (part == 0)
+					{
+						for (int q = 1; q < S; q++)
+						{
+#pragma unroll
+							for (int t = 0; t < TPT; t++)
+							{
+								int slot = (q * (NT / 32 / S) + group) * 64 + t * 32 + lane;
+								totR[t] = cadd(totR[t], red[2 * slot]);
+								totS[t] = cadd(totS[t], red[2 * slot + 1]);
+							}
+						}
+					}
+					__syncthreads();
+				}
 
-				/* the Aberth update of each target (warp-uniform calls) */
+				/* locate the targets; the star sums of the off-field ones are
+				   computed by the whole CTA rather than by their own warps */
+				int leaf_t[TPT], slot_t[TPT];
 #pragma unroll
 				for (int t = 0; t < TPT; t++)
 				{
-					double2 S = make_double2(2 * totS[t].x - totR[t].x, 2 * totS[t].y - totR[t].y);
-					if (aberth_update_warp<MIXED>(F, master, fin, valid[t], tid_a[t], S, disc_exact, cphi, sphi) == 2)
-						atomicOr(&s_nan, 2);
+					leaf_t[t] = 0;
+					slot_t[t] = -1;
+					if (part == 0 && valid[t])
+					{
+						const double2 z = master[tid_a[t]];
+						leaf_t[t] = find_leaf(F, z);
+						if (leaf_t[t] < 0)
+						{
+							const int q = atomicAdd(&s_noff, 1);
+							if (q < OFF_CAP)
+							{
+								s_offz[q] = z;
+								slot_t[t] = q;
+							}
+						}
+					}
+				}
+				__syncthreads();
+				const int K = min(s_noff, OFF_CAP);
+				offfield_sums_cta<MIXED, false, true>(F, s_offz, K, s_offs, red_off);
+
+				/* the Aberth update of each target (warp-uniform calls) */
+				if (part == 0)
+				{
+#pragma unroll
+					for (int t = 0; t < TPT; t++)
+					{
+						double2 Sg = make_double2(2 * totS[t].x - totR[t].x, 2 * totS[t].y - totR[t].y);
+						const bool have = slot_t[t] >= 0;
+						const NearSums off = have ? s_offs[slot_t[t]] : zero_sums();
+						if (aberth_update_warp<MIXED>(F, master, fin, valid[t], tid_a[t], leaf_t[t], have, off, Sg, disc_exact,
+								cphi, sphi) == 2)
+							s_nan_step = 1;
+					}
 				}
 			}
 			if (threadIdx.x == 0)
 			{
 				int mine = 0;
-				for (int tile = crank; tile < ntiles; tile += csize) mine += min(TILE, total - tile * TILE);
+				for (int tile = crank; tile < ntiles; tile += csize) mine += min(TT, total - tile * TT);
 				s_upd += mine;
 				s_terms += (unsigned long long)mine * (unsigned long long)(R - 1 + N);
 			}
@@ -401,8 +575,26 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 			const int a = a0 + threadIdx.x;
 			const bool v = a < o1;
 			double2 z = v ? master[a] : make_double2(0, 0);
+			const int leaf = v ? find_leaf(F, z) : 0;
+			int slot = -1;
+			if (threadIdx.x == 0) s_noff = 0;
+			__syncthreads();
+			if (v && leaf < 0)
+			{
+				const int q = atomicAdd(&s_noff, 1);
+				if (q < OFF_CAP)
+				{
+					s_offz[q] = z;
+					slot = q;
+				}
+			}
+			__syncthreads();
+			const int K = min(s_noff, OFF_CAP);
+			if (sO.mu) offfield_sums_cta<MIXED, true, true>(F, s_offz, K, s_offs, red_off);
+			else offfield_sums_cta<MIXED, true, false>(F, s_offz, K, s_offs, red_off);
 			size_t out = ((size_t)(v ? a : 0) * nb + c) * sO.cols + k;
-			point_epilogue_warp(F, sO, v, z, out, cphi, sphi, &s_maxerr, &s_nan);
+			const NearSums off = slot >= 0 ? s_offs[slot] : zero_sums();
+			if (!point_epilogue_warp<MIXED>(F, sO, v, z, leaf, slot >= 0, off, out, cphi, sphi, &s_maxerr)) s_nan_err = 1;
 			if (!v) continue;
 			if (!fin[a]) atomicAdd(&s_unconv, 1ull);
 			if (initial)
@@ -431,7 +623,8 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 	{
 		unsigned long long* st = sO.stats;
 		atomicMax(&st[0], (unsigned long long)__double_as_longlong(s_maxerr));
-		if (s_nan) atomicOr(&st[1], (unsigned long long)s_nan);
+		const unsigned long long flags = (s_nan_err ? 1ull : 0ull) | (s_nan_step ? 2ull : 0ull);
+		if (flags) atomicOr(&st[1], flags);
 		atomicAdd(&st[2], s_upd);
 		atomicAdd(&st[3], s_terms);
 		if (initial)

@@ -111,11 +111,19 @@ __global__ void seed_roots_kernel(int nstars, int nroots, int nrows, const doubl
 	}
 }
 
-/* FP32 hi/lo form of the star positions, the poles of the Aberth sums */
-__global__ void star_hilo_kernel(int n, const double2* __restrict__ pos, float4* __restrict__ out)
+/* FP32 hi/lo form of the star positions (the poles of the Aberth sums) and,
+   when mass is given, of the masses */
+__global__ void star_hilo_kernel(int n, const double2* __restrict__ pos, float4* __restrict__ out,
+	const double* __restrict__ mass, float2* __restrict__ mass_out)
 {
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i < n) out[i] = split_hilo(pos[i]);
+	if (i >= n) return;
+	out[i] = split_hilo(pos[i]);
+	if (mass)
+	{
+		float h = __double2float_rn(mass[i]);
+		mass_out[i] = make_float2(h, __double2float_rn(mass[i] - (double)h));
+	}
 }
 
 void launch_generate_stars(cudaStream_t s, int n, int seed, int rectangular, double2 corner, double corner_abs,
@@ -137,9 +145,9 @@ void launch_seed_roots(cudaStream_t s, int nstars, int nroots, int nrows, const 
 	seed_roots_kernel<<<blocks, 256, 0, s>>>(nstars, nroots, nrows, pos, corner_abs, master, snap32, snap64);
 }
 
-void launch_star_hilo(cudaStream_t s, int n, const double2* pos, float4* out)
+void launch_star_hilo(cudaStream_t s, int n, const double2* pos, float4* out, const double* mass, float2* mass_out)
 {
-	star_hilo_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, pos, out);
+	star_hilo_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, pos, out, mass, mass_out);
 }
 
 } /* namespace ccf */
