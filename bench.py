@@ -304,7 +304,7 @@ def main() -> None:
             "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": ws, "steps": args.steps,
             "warmup": max(3, args.warmup), "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32+f64 (FP32 correction sums, FP64 root function)" if args.precision == "mixed" else "f64",
+            "dtype": "f32+df32+f64 (FP32 correction sums, double-float f and caustics, FP64 off the corner circle)" if args.precision == "mixed" else "f64",
             "data": "synthetic (seeded star field)",
             "config": {"workload": args.workload, **cfg, "precision": args.precision,
                        "l2": "flushed before every timed step (256 MiB write)", "parallelism": f"replicas x{ws}"},

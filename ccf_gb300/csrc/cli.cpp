@@ -114,7 +114,7 @@ static void display_usage(char* name)
 		<< "  -o,--outfile_prefix        Specify the prefix to be used in output\n"
 		<< "                             filenames. Default value: " << ccf.outfile_prefix << "\n"
 		<< "  -pr,--precision            Root solver arithmetic: mixed (FP32 correction sums,\n"
-		<< "                             FP64 critical-curve function) or fp64.\n"
+		<< "                             double-float critical-curve function) or fp64.\n"
 		<< "                             Default value: mixed\n"
 		<< "  -d,--device                CUDA device ordinal. Default value: 0\n";
 }

@@ -543,6 +543,8 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 	CCF_TRY(P.fin_cont.ensure(ncont), "cudaMalloc(roots)");
 	CCF_TRY(P.list_init.ensure(ninit), "cudaMalloc(roots)");
 	CCF_TRY(P.list_cont.ensure(ncont), "cudaMalloc(roots)");
+	CCF_TRY(P.fval_init.ensure(2 * ninit), "cudaMalloc(roots)");
+	CCF_TRY(P.fval_cont.ensure(2 * ncont), "cudaMalloc(roots)");
 	if (mixed)
 	{
 		CCF_TRY(P.snap32_init.ensure(ninit), "cudaMalloc(roots)");
@@ -656,6 +658,7 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 	A.snap64 = mixed ? nullptr : P.snap64_init.ptr;
 	A.fin = P.fin_init.ptr;
 	A.list = P.list_init.ptr;
+	A.fval = P.fval_init.ptr;
 	CCF_TRY(launch_solve(s, A, mixed, true), "find_initial_roots");
 	for (Field* f : fields) CCF_TRY(cudaEventRecord(f->ev[4], s), "event");
 	if (verbose >= 1) std::cout << "Finding critical curve positions...\n";
@@ -667,6 +670,7 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 	A.snap64 = mixed ? nullptr : P.snap64_cont.ptr;
 	A.fin = P.fin_cont.ptr;
 	A.list = P.list_cont.ptr;
+	A.fval = P.fval_cont.ptr;
 	CCF_TRY(launch_solve(s, A, mixed, false), "find_ccs");
 	for (Field* f : fields) CCF_TRY(cudaEventRecord(f->ev[5], s), "event");
 	CCF_TRY(cudaStreamSynchronize(s), "solver");

@@ -135,6 +135,7 @@ struct SolverPools
 	DBuf<float4> snap32_init, snap32_cont;
 	DBuf<unsigned char> fin_init, fin_cont;
 	DBuf<int> list_init, list_cont;
+	DBuf<double2> fval_init, fval_cont;   /* f, f' per root */
 	DBuf<RowDesc> rows_init, rows_cont;
 	DBuf<FieldView> views;
 	DBuf<FieldOut> outs;

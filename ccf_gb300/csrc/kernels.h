@@ -86,6 +86,7 @@ struct SolveArgs
 	double2* snap64;
 	unsigned char* fin;
 	int* list;
+	double2* fval;         /* [2 (row base + root) + {0, 1}]: f and f' of the sweep's active roots */
 	const float4* const* star_hilo;   /* per field, FP32 hi/lo stars (mixed) */
 	int* error;
 };

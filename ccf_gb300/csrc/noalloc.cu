@@ -11,7 +11,7 @@ flags, the active-root list and the launch descriptors) lives in the
 file-scope device array below instead of in buffers the engine allocates.
 The array holds NOALLOC_SCRATCH_BYTES (8 MiB); every GPU that loads the
 library keeps it until the process exits.  A row of R roots needs about
-37 R bytes plus 8 KiB, so R may be up to about 220 000; larger rows are
+69 R bytes plus 8 KiB, so R may be up to about 120 000; larger rows are
 rejected with CCF_ERR_INVALID_ARGUMENT.
 
 All calls share the one array and it keeps the last call's contents; calls
@@ -96,7 +96,8 @@ extern "C" ccf_status ccf_continue_branch_noalloc(ccf_handle* h, int branch, int
 	const size_t o_snap = align256(o_master + (size_t)R * sizeof(double2));
 	const size_t o_fin = align256(o_snap + (size_t)R * (mixed ? sizeof(float4) : sizeof(double2)));
 	const size_t o_list = align256(o_fin + (size_t)R);
-	const size_t need = align256(o_list + (size_t)R * sizeof(int));
+	const size_t o_fval = align256(o_list + (size_t)R * sizeof(int));
+	const size_t need = align256(o_fval + 2 * (size_t)R * sizeof(double2));
 	if (need > NOALLOC_SCRATCH_BYTES)
 	{
 		ccf_internal_set_error(h, "Error. A row of " + std::to_string(R) + " roots needs " + std::to_string(need) +
@@ -168,6 +169,7 @@ extern "C" ccf_status ccf_continue_branch_noalloc(ccf_handle* h, int branch, int
 	A.snap64 = mixed ? nullptr : (double2*)(base + o_snap);
 	A.fin = base + o_fin;
 	A.list = (int*)(base + o_list);
+	A.fval = (double2*)(base + o_fval);
 	A.star_hilo = (const float4* const*)(base + o_hilo);
 	A.error = nullptr;
 	e = ccf::launch_solve(s, A, mixed, false);

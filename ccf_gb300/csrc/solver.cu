@@ -153,56 +153,45 @@ CCF_D double row_phi(int c, int nb, int nphi, int side, int j)
 	return side == 0 ? phi0 - dphi : phi0 + dphi;
 }
 
-/* One Aberth step for the target of every lane with valid set, given its
-   leaf and its correction sum S; returns 0, 1 when the root became final, 2
-   when the step was not finite (the root is then frozen).  An off-field
-   target (leaf < 0) takes its star sums from off when have_off is set (the
-   CTA computed them) and otherwise from the whole warp -- so all 32 lanes of
-   the warp must call it.  Not inlined: the evaluation needs its registers
-   once, not once per unrolled target. */
-template <bool MIXED>
-__device__ __noinline__ int aberth_update_warp(const FieldView& F, double2* __restrict__ master, unsigned char* __restrict__ fin,
-	bool valid, int a, int leaf, bool have_off, NearSums off, double2 S, bool disc_exact, double cphi, double sphi)
+/* f and f' of a root */
+struct FdF
 {
-	double2 z = valid ? master[a] : make_double2(0, 0);
+	double2 f, df;
+};
+
+/* f(z; phi) and f'(z) for the root of every lane with valid set, given its
+   leaf.  An off-field root (leaf < 0) takes its star sums from off when
+   have_off is set (the CTA computed them) and otherwise from the whole warp
+   -- so all 32 lanes of the warp must call it.  Not inlined: the evaluation
+   needs its registers once, not in every caller's frame. */
+template <bool MIXED>
+__device__ __noinline__ FdF eval_fdf_warp(const FieldView& F, bool valid, double2 z, int leaf, bool have_off, NearSums off,
+	double cphi, double sphi)
+{
 	NearSums ns = have_off ? off : zero_sums();
 	if (!MIXED && valid && leaf >= 0) ns = leaf_sums<false, true>(F, leaf, z);
 	offfield_sums_warp<false, true>(F, valid && leaf < 0 && !have_off, z, ns);
-	if (!valid) return 0;
-	if (disc_exact)
-	{
-		double2 iz = cinv(z);
-		S.x += 2 * iz.x;
-		S.y += 2 * iz.y;
-	}
-	double2 f, df;
+	FdF r;
+	r.f = make_double2(0, 0);
+	r.df = make_double2(0, 0);
+	if (!valid) return r;
 	if constexpr (MIXED)
 	{
 		/* f in double-float on the FP32 pipe, off-field points included */
-		f = eval_f_df(F, leaf, z, cphi, sphi, ns);
-		float2 d32 = eval_df32(F, leaf, z, ns.s3);
-		df = make_double2(d32.x, d32.y);
+		r.f = eval_f_df(F, leaf, z, cphi, sphi, ns);
+		const float2 d32 = eval_df32(F, leaf, z, ns.s3);
+		r.df = make_double2(d32.x, d32.y);
 	}
 	else
 	{
-		eval_f64<true>(F, leaf, z, cphi, sphi, ns, f, df);
+		eval_f64<true>(F, leaf, z, cphi, sphi, ns, r.f, r.df);
 	}
-	double2 den = cadd(df, cmul(f, S));
-	double2 znew = csub(z, cdiv(f, den));
-	if (isfinite(znew.x) && isfinite(znew.y))
-	{
-		double norm = hypot(znew.x - z.x, znew.y - z.y) / F.theta;
-		master[a] = znew;
-		if (norm < 0.000000001)
-		{
-			fin[a] = 1;
-			return 1;
-		}
-		return 0;
-	}
-	fin[a] = 1;
-	return 2;
+	return r;
 }
+
+/* A root is final once its step is below this many theta_star (the
+   reference's test, include/ccf_functions.cuh:385). */
+constexpr double STEP_TOL = 0.000000001;
 
 /* outputs of one final root per lane: position, 1/mu bound, caustic,
    length scale; returns false when the 1/mu bound is not finite.  All 32
@@ -288,8 +277,13 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 	double2* __restrict__ master = A.master + base;
 	unsigned char* __restrict__ fin = A.fin + base;
 	int* __restrict__ list = A.list + base;
-	const SrcT* __restrict__ rsrc;
-	const SrcT* __restrict__ ssrc;
+	double2* fval = A.fval + 2 * base;
+	unsigned long long n_eval = 0;   /* f evaluations of this thread */
+	/* the row snapshot is rewritten between sweeps by the CTAs of the cluster:
+	   no __restrict__ (it would allow the non-coherent read-only path), and
+	   its loads go through L2 (__ldcg here, cp.async.cg for the sources) */
+	const SrcT* rsrc;
+	const SrcT* ssrc;
 	if constexpr (MIXED)
 	{
 		rsrc = A.snap32 + base;
@@ -317,6 +311,58 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 		int it = 0;
 		while (true)
 		{
+			/* Newton check: f and f' of this CTA's active roots, at the positions
+			   the sweep starts from.  Close to a simple zero the Aberth step
+			   f / (f' + f S) is the Newton step f / f' to a relative f S / f'
+			   (~1e-6 and below there), so a root whose Newton step is already
+			   under the tolerance takes that step and is final without its
+			   O(R + N) correction sums -- the sweep that only confirms a
+			   converged root costs one evaluation.  The others keep f and f' for
+			   their Aberth step after the sums. */
+			if (it < max_it)
+			{
+				for (int a0 = o0; a0 < o1; a0 += NT)
+				{
+					/* uniform trip count: the CTA-wide and warp-wide calls below */
+					const int a = a0 + threadIdx.x;
+					const bool v = a < o1 && !fin[a];
+					const double2 z = v ? master[a] : make_double2(0, 0);
+					const int leaf = v ? find_leaf(F, z) : 0;
+					int slot = -1;
+					if (threadIdx.x == 0) s_noff = 0;
+					__syncthreads();
+					if (v && leaf < 0)
+					{
+						const int q = atomicAdd(&s_noff, 1);
+						if (q < OFF_CAP)
+						{
+							s_offz[q] = z;
+							slot = q;
+						}
+					}
+					__syncthreads();
+					const int K = min(s_noff, OFF_CAP);
+					offfield_sums_cta<MIXED, false, true>(F, s_offz, K, s_offs, red_off);
+					const NearSums off = slot >= 0 ? s_offs[slot] : zero_sums();
+					const FdF e = eval_fdf_warp<MIXED>(F, v, z, leaf, slot >= 0, off, cphi, sphi);
+					if (v)
+					{
+						n_eval++;
+						const double2 step = cdiv(e.f, e.df);
+						if (isfinite(step.x) && isfinite(step.y) && hypot(step.x, step.y) < STEP_TOL * F.theta)
+						{
+							master[a] = csub(z, step);
+							fin[a] = 1;
+						}
+						else
+						{
+							fval[2 * a] = e.f;
+							fval[2 * a + 1] = e.df;
+						}
+					}
+				}
+			}
+
 			/* compact this CTA's active roots into its segment of the row list */
 			if (threadIdx.x == 0) s_fill = 0;
 			__syncthreads();
@@ -363,9 +409,6 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 			const int ntiles = (total + TT - 1) / TT;
 			for (int tile = crank; tile < ntiles; tile += csize)
 			{
-				/* the barriers of the chunk loop order this reset before any
-				   target of the tile is counted */
-				if (threadIdx.x == 0) s_noff = 0;
 				int tid_a[TPT];
 				bool valid[TPT];
 				SrcT zs[TPT];
@@ -384,8 +427,8 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 						a = list[seg0 + (g - s_pre[r])];
 					}
 					tid_a[t] = a;
-					if constexpr (MIXED) zs[t] = valid[t] ? rsrc[a] : make_float4(0, 0, 0, 0);
-					else zs[t] = valid[t] ? rsrc[a] : make_double2(0, 0);
+					if constexpr (MIXED) zs[t] = valid[t] ? __ldcg(rsrc + a) : make_float4(0, 0, 0, 0);
+					else zs[t] = valid[t] ? __ldcg(rsrc + a) : make_double2(0, 0);
 					totR[t] = make_double2(0, 0);
 					totS[t] = make_double2(0, 0);
 				}
@@ -504,45 +547,35 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 					__syncthreads();
 				}
 
-				/* locate the targets; the star sums of the off-field ones are
-				   computed by the whole CTA rather than by their own warps */
-				int leaf_t[TPT], slot_t[TPT];
-#pragma unroll
-				for (int t = 0; t < TPT; t++)
-				{
-					leaf_t[t] = 0;
-					slot_t[t] = -1;
-					if (part == 0 && valid[t])
-					{
-						const double2 z = master[tid_a[t]];
-						leaf_t[t] = find_leaf(F, z);
-						if (leaf_t[t] < 0)
-						{
-							const int q = atomicAdd(&s_noff, 1);
-							if (q < OFF_CAP)
-							{
-								s_offz[q] = z;
-								slot_t[t] = q;
-							}
-						}
-					}
-				}
-				__syncthreads();
-				const int K = min(s_noff, OFF_CAP);
-				offfield_sums_cta<MIXED, false, true>(F, s_offz, K, s_offs, red_off);
-
-				/* the Aberth update of each target (warp-uniform calls) */
+				/* the Aberth step of each target from the f and f' of the Newton
+				   check (the sweep's starting positions, as the sums) */
 				if (part == 0)
 				{
 #pragma unroll
 					for (int t = 0; t < TPT; t++)
 					{
+						if (!valid[t]) continue;
+						const int a = tid_a[t];
+						const double2 z = __ldcg(master + a);
+						const double2 f = __ldcg(fval + 2 * a), df = __ldcg(fval + 2 * a + 1);
 						double2 Sg = make_double2(2 * totS[t].x - totR[t].x, 2 * totS[t].y - totR[t].y);
-						const bool have = slot_t[t] >= 0;
-						const NearSums off = have ? s_offs[slot_t[t]] : zero_sums();
-						if (aberth_update_warp<MIXED>(F, master, fin, valid[t], tid_a[t], leaf_t[t], have, off, Sg, disc_exact,
-								cphi, sphi) == 2)
+						if (disc_exact)
+						{
+							const double2 iz = cinv(z);
+							Sg.x += 2 * iz.x;
+							Sg.y += 2 * iz.y;
+						}
+						const double2 znew = csub(z, cdiv(f, cadd(df, cmul(f, Sg))));
+						if (isfinite(znew.x) && isfinite(znew.y))
+						{
+							master[a] = znew;
+							if (hypot(znew.x - z.x, znew.y - z.y) < STEP_TOL * F.theta) fin[a] = 1;
+						}
+						else
+						{
+							fin[a] = 1;
 							s_nan_step = 1;
+						}
 					}
 				}
 			}
@@ -550,7 +583,6 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 			{
 				int mine = 0;
 				for (int tile = crank; tile < ntiles; tile += csize) mine += min(TT, total - tile * TT);
-				s_upd += mine;
 				s_terms += (unsigned long long)mine * (unsigned long long)(R - 1 + N);
 			}
 			cluster.sync();
@@ -618,6 +650,7 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 		cluster.sync();
 	}
 
+	if (n_eval) atomicAdd(&s_upd, n_eval);
 	__syncthreads();
 	if (threadIdx.x == 0)
 	{

@@ -47,8 +47,10 @@ typedef enum ccf_status
 typedef enum ccf_precision
 {
 	CCF_PRECISION_FP64 = 0,  /* all solver arithmetic in FP64 */
-	CCF_PRECISION_MIXED = 1  /* FP32 Aberth correction sums, FP64 critical-curve
-	                            function, residual and caustic map */
+	CCF_PRECISION_MIXED = 1  /* FP32 Aberth correction sums; critical-curve
+	                            function, residual and caustic map in double-float
+	                            (two FP32 numbers, ~48 bits) within the corner
+	                            circle and FP64 outside; length scales in FP64 */
 } ccf_precision;
 
 /* Parameters.  The first block mirrors the public fields of CCF<T> with the
@@ -226,7 +228,7 @@ ccf_status ccf_eval_points(ccf_handle* h, int n, const double* z, const double* 
    real-time loop that must not take the allocator's locks or synchronise
    implicitly.  The solver's per-row scratch sits in a fixed 8 MiB device
    array built into the library (held by every GPU that loads it until the
-   process exits), which limits a row to about 220 000 roots; larger rows are
+   process exits), which limits a row to about 120 000 roots; larger rows are
    rejected with CCF_ERR_INVALID_ARGUMENT.
    start_roots: num_roots complex roots (device memory) at the branch centre.
    ccs, errs, caustics: device arrays in the ccf_get_results layout of the
