@@ -122,6 +122,23 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# DRAM bytes (read + write) of the continuation launch per continuation point,
+# from the ncu capture summarised in
+# profiles/solve_kernel_cont_n2000_salpeter_phi512.md: 115.3 MB for the
+# 4056 * 512 points of that launch.  The traffic is the outputs plus snapshot
+# and star reads, so it grows with the points written.
+CONT_DRAM_BYTES_PER_POINT = 115.3e6 / (4056 * 512)
+
+
+def hbm_peak_gbs() -> float | None:
+    """Measured HBM copy bandwidth of the GB300s (MEASURED_PEAKS.json)."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"])
+    except Exception:  # noqa: BLE001
+        return None
+
+
 def measure_peaks() -> dict:
     exe = os.path.join(ROOT, "ccf_gb300", "lib", "ccf_peaks")
     try:
@@ -279,6 +296,8 @@ def main() -> None:
     flops = algorithmic_flops(info, continuation_only=True)
     achieved = flops / t_cont / 1e12 if t_cont > 0 else 0.0
     peak32 = peaks.get("fp32_tflops")
+    traffic = CONT_DRAM_BYTES_PER_POINT * info["num_roots"] * cfg["num_phi"]
+    hbm_peak = hbm_peak_gbs()
 
     fp64 = None
     if args.precision == "mixed" and args.fp64_steps > 0:
@@ -311,10 +330,15 @@ def main() -> None:
             "e2e": {"value": points * args.steps * ws / t_e2e, "unit": "points/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
-                         "frac": (achieved / peak32) if peak32 else None, "traffic": None,
+                         "frac": (achieved / peak32) if peak32 else None, "traffic": traffic,
                          "kernel": "solve_kernel (phi continuation)", "kernel_share_of_step": cont_share,
                          "peak_source": "ccf_gb300/lib/ccf_peaks (FFMA chains, measured)",
-                         "fp64_peak_tflops": peaks.get("fp64_tflops")},
+                         "fp64_peak_tflops": peaks.get("fp64_tflops"),
+                         "traffic_source": "per-point DRAM bytes of the ncu capture in "
+                                           "profiles/solve_kernel_cont_n2000_salpeter_phi512.md, scaled by points",
+                         "hbm_gbs": traffic / t_cont / 1e9 if t_cont > 0 else None,
+                         "hbm_peak_gbs": hbm_peak, "hbm_frac": (traffic / t_cont / 1e9 / hbm_peak)
+                         if (t_cont > 0 and hbm_peak) else None},
             "fp64_plain": fp64,
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
