@@ -18,6 +18,7 @@ STATUS_NAMES = {
     4: "CCF_ERR_OUT_OF_MEMORY", 5: "CCF_ERR_IO", 6: "CCF_ERR_NOT_RUN", 7: "CCF_ERR_NUMERIC",
     8: "CCF_ERR_TIMEOUT", 9: "CCF_ERR_BUDGET",
 }
+STATUS_CODES = {name: code for code, name in STATUS_NAMES.items()}
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 
@@ -113,8 +114,59 @@ EXPORTED = [
     "ccf_abi_version", "ccf_default_params", "ccf_create", "ccf_destroy", "ccf_set_params", "ccf_get_params",
     "ccf_set_stars", "ccf_run", "ccf_save", "ccf_get_info", "ccf_get_results", "ccf_get_device_results",
     "ccf_last_error", "ccf_derive_params", "ccf_run_batch", "ccf_write_star_file", "ccf_eval_points",
-    "ccf_continue_branch_noalloc",
+    "ccf_continue_branch_noalloc", "ccf_estimate_device_bytes", "ccf_batch_submit", "ccf_batch_poll",
+    "ccf_batch_wait", "ccf_batch_destroy", "ccf_server_create", "ccf_server_submit", "ccf_server_wait",
+    "ccf_server_request_info", "ccf_server_handle", "ccf_server_release", "ccf_server_get_stats",
+    "ccf_server_destroy",
 ]
+
+REQUEST_QUEUED, REQUEST_RUNNING, REQUEST_DONE, REQUEST_FAILED, REQUEST_REJECTED = range(5)
+
+
+class CcfServerConfig(ctypes.Structure):
+    _fields_ = [
+        ("device", ctypes.c_int),
+        ("slots", ctypes.c_int),
+        ("hbm_budget", ctypes.c_ulonglong),
+        ("verbose", ctypes.c_int),
+        ("reserved", ctypes.c_int * 7),
+    ]
+
+
+class CcfRequestInfo(ctypes.Structure):
+    _fields_ = [
+        ("state", ctypes.c_int),
+        ("status", ctypes.c_int),
+        ("deferred", ctypes.c_int),
+        ("reserved0", ctypes.c_int),
+        ("bytes", ctypes.c_ulonglong),
+        ("t_submit", ctypes.c_double),
+        ("t_start", ctypes.c_double),
+        ("t_end", ctypes.c_double),
+        ("reserved", ctypes.c_double * 4),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_ if not name.startswith("reserved")}
+
+
+class CcfServerStats(ctypes.Structure):
+    _fields_ = [
+        ("submitted", ctypes.c_longlong),
+        ("admitted", ctypes.c_longlong),
+        ("completed", ctypes.c_longlong),
+        ("failed", ctypes.c_longlong),
+        ("rejected", ctypes.c_longlong),
+        ("deferred", ctypes.c_longlong),
+        ("queued", ctypes.c_longlong),
+        ("running", ctypes.c_longlong),
+        ("bytes_in_use", ctypes.c_ulonglong),
+        ("hbm_budget", ctypes.c_ulonglong),
+        ("reserved", ctypes.c_double * 4),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_ if name != "reserved"}
 
 _lib = None
 _lock = threading.Lock()
@@ -156,6 +208,22 @@ def load(path: str | None = None):
         L.ccf_eval_points.argtypes = [H, ctypes.c_int, dp, dp, dp, dp, dp, dp, dp]
         vp = ctypes.c_void_p
         L.ccf_continue_branch_noalloc.argtypes = [H, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp]
+        ull = ctypes.c_ulonglong
+        L.ccf_estimate_device_bytes.argtypes = [PP, ctypes.POINTER(ull)]
+        L.ccf_batch_submit.argtypes = [ctypes.POINTER(H), ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp)]
+        L.ccf_batch_poll.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
+        L.ccf_batch_wait.argtypes = [vp]
+        L.ccf_batch_destroy.argtypes = [vp]
+        L.ccf_batch_destroy.restype = None
+        L.ccf_server_create.argtypes = [ctypes.POINTER(CcfServerConfig), ctypes.POINTER(vp)]
+        L.ccf_server_submit.argtypes = [vp, PP, ctypes.POINTER(ctypes.c_longlong)]
+        L.ccf_server_wait.argtypes = [vp, ctypes.c_longlong, ctypes.c_double]
+        L.ccf_server_request_info.argtypes = [vp, ctypes.c_longlong, ctypes.POINTER(CcfRequestInfo)]
+        L.ccf_server_handle.argtypes = [vp, ctypes.c_longlong, ctypes.POINTER(H)]
+        L.ccf_server_release.argtypes = [vp, ctypes.c_longlong]
+        L.ccf_server_get_stats.argtypes = [vp, ctypes.POINTER(CcfServerStats)]
+        L.ccf_server_destroy.argtypes = [vp]
+        L.ccf_server_destroy.restype = None
         for name in EXPORTED:
             fn = getattr(L, name)
             if fn.restype is ctypes.c_int and name not in ("ccf_abi_version",):

@@ -77,7 +77,7 @@ class CCF:
 
     def __del__(self):
         try:
-            if getattr(self, "_h", None) and self._h.value:
+            if getattr(self, "_owned", True) and getattr(self, "_h", None) and self._h.value:
                 self._L.ccf_destroy(self._h)
                 self._h = ctypes.c_void_p()
         except Exception:
@@ -125,6 +125,15 @@ class CCF:
 
     def last_error(self) -> str:
         return self._L.ccf_last_error(self._h).decode()
+
+    def estimate_device_bytes(self) -> int:
+        """Device memory a run with the current parameters holds (upper estimate)."""
+        p = self._params()
+        out = ctypes.c_ulonglong()
+        rc = self._L.ccf_estimate_device_bytes(ctypes.byref(p), ctypes.byref(out))
+        if rc != 0:
+            raise CCFError(rc, "ccf_estimate_device_bytes failed")
+        return int(out.value)
 
     # ---- the reference's API ----
     def run(self, verbose: int = 0) -> bool:
@@ -201,18 +210,141 @@ def run_batch(fields: list[CCF], verbose: int = 0) -> bool:
     return rc == 0
 
 
-def derive_params(**kw) -> dict:
-    """Checks and derived parameters on the host (no GPU needed)."""
+class BatchJob:
+    """A batch of fields running on a host thread (ccf_batch_submit)."""
+
+    def __init__(self, fields: list[CCF], verbose: int = 0):
+        self._L = fields[0]._L
+        self.fields = fields
+        for f in fields:
+            f._push()
+        arr = (ctypes.c_void_p * len(fields))(*[f._h.value for f in fields])
+        self._b = ctypes.c_void_p()
+        rc = self._L.ccf_batch_submit(arr, len(fields), int(verbose), ctypes.byref(self._b))
+        if rc != 0:
+            raise CCFError(rc, "ccf_batch_submit failed")
+
+    def done(self) -> bool:
+        d = ctypes.c_int()
+        self._L.ccf_batch_poll(self._b, ctypes.byref(d))
+        return bool(d.value)
+
+    def wait(self) -> bool:
+        rc = self._L.ccf_batch_wait(self._b)
+        for f in self.fields:
+            f.last_status = rc
+        return rc == 0
+
+    def __del__(self):
+        try:
+            if self._b.value:
+                self._L.ccf_batch_destroy(self._b)
+                self._b = ctypes.c_void_p()
+        except Exception:
+            pass
+
+
+def submit_batch(fields: list[CCF], verbose: int = 0) -> BatchJob:
+    """run_batch without blocking: poll or wait on the returned job."""
+    return BatchJob(fields, verbose)
+
+
+def _bare(**kw) -> CCF:
+    """A CCF parameter holder without a native handle."""
     c = CCF.__new__(CCF)
     c._L = _lib.load()
+    c._h = ctypes.c_void_p()
+    c._owned = False
     for k, (v, _) in _FIELDS.items():
         setattr(c, k, v)
     c.precision, c.output_float, c.max_iters_init, c.max_iters_step, c.exact_binomials, c.device = \
         "mixed", 0, 300, 60, 0, 0
+    c._stars_keep = None
+    c.last_status = 0
     for k, v in kw.items():
         if k == "mass_function":
             k = "mass_function_str"
+        if not hasattr(c, k):
+            raise AttributeError(k)
         setattr(c, k, v)
+    return c
+
+
+class Server:
+    """Request loop over one GPU (ccf_server_*): requests are queued in arrival
+    order and admitted while a slot is free and the device memory of the
+    admitted requests stays within hbm_budget; each runs on its own stream, so
+    concurrent requests overlap on the device.  Results stay on the device
+    until release(id)."""
+
+    def __init__(self, slots: int = 4, hbm_budget: float = 60e9, device: int = 0, verbose: int = 0):
+        self._L = _lib.load()
+        cfg = _lib.CcfServerConfig()
+        cfg.device, cfg.slots, cfg.hbm_budget, cfg.verbose = int(device), int(slots), int(hbm_budget), int(verbose)
+        self._s = ctypes.c_void_p()
+        rc = self._L.ccf_server_create(ctypes.byref(cfg), ctypes.byref(self._s))
+        if rc != 0:
+            raise CCFError(rc, "ccf_server_create failed")
+        self._kw = {}
+
+    def submit(self, **kw) -> int:
+        """Queue a field solve with CCF's parameters; returns its request id."""
+        c = _bare(**kw)
+        p = c._params()
+        rid = ctypes.c_longlong()
+        rc = self._L.ccf_server_submit(self._s, ctypes.byref(p), ctypes.byref(rid))
+        if rc != 0:
+            raise CCFError(rc, "ccf_server_submit failed")
+        self._kw[rid.value] = dict(kw)
+        return rid.value
+
+    def wait(self, rid: int, timeout: float | None = None) -> int:
+        """Status of the request once finished (CCF_ERR_TIMEOUT while running)."""
+        return self._L.ccf_server_wait(self._s, rid, -1.0 if timeout is None else float(timeout))
+
+    def info(self, rid: int) -> dict:
+        i = _lib.CcfRequestInfo()
+        rc = self._L.ccf_server_request_info(self._s, rid, ctypes.byref(i))
+        if rc != 0:
+            raise CCFError(rc, "unknown request")
+        return i.as_dict()
+
+    def field(self, rid: int) -> CCF:
+        """The finished request as a CCF (results(), info(), save()); valid until release(rid)."""
+        h = ctypes.c_void_p()
+        rc = self._L.ccf_server_handle(self._s, rid, ctypes.byref(h))
+        if rc != 0:
+            raise CCFError(rc, "request has no field")
+        c = _bare(**self._kw[rid])
+        c._h = h
+        return c
+
+    def release(self, rid: int) -> None:
+        rc = self._L.ccf_server_release(self._s, rid)
+        if rc != 0:
+            raise CCFError(rc, "ccf_server_release failed")
+        self._kw.pop(rid, None)
+
+    def stats(self) -> dict:
+        st = _lib.CcfServerStats()
+        self._L.ccf_server_get_stats(self._s, ctypes.byref(st))
+        return st.as_dict()
+
+    def close(self) -> None:
+        if self._s.value:
+            self._L.ccf_server_destroy(self._s)
+            self._s = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def derive_params(**kw) -> dict:
+    """Checks and derived parameters on the host (no GPU needed)."""
+    c = _bare(**kw)
     p = c._params()
     info = _lib.CcfInfo()
     msg = ctypes.create_string_buffer(512)

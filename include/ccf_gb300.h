@@ -242,6 +242,93 @@ ccf_status ccf_eval_points(ccf_handle* h, int n, const double* z, const double* 
 ccf_status ccf_continue_branch_noalloc(ccf_handle* h, int branch, int side, int num_steps, const double* start_roots,
 	double* ccs, double* errs, double* caustics, void* stream);
 
+/* Device memory a run with parameters p will hold (stars, tree, FMM and leaf
+   records, solver rows, outputs), an upper estimate used for admission.  No
+   reference counterpart (the reference allocates managed memory as it goes,
+   include/ccf.cuh:131-143). */
+ccf_status ccf_estimate_device_bytes(const ccf_params* p, unsigned long long* bytes);
+
+/* ---------------- asynchronous batches ----------------
+   ccf_run_batch on a host thread: submit returns at once, poll / wait read
+   the outcome.  The handles must stay alive and untouched until the batch is
+   waited for.  No reference counterpart (one field per process there). */
+typedef struct ccf_batch ccf_batch;
+ccf_status ccf_batch_submit(ccf_handle** handles, int n, int verbose, ccf_batch** out);
+/* *done = 1 once the batch has finished */
+ccf_status ccf_batch_poll(ccf_batch* b, int* done);
+/* waits and returns the batch's ccf_run_batch status */
+ccf_status ccf_batch_wait(ccf_batch* b);
+/* waits if needed, then frees the batch object (not the handles) */
+void ccf_batch_destroy(ccf_batch* b);
+
+/* ---------------- serving ----------------
+   A request loop over one GPU.  Requests (parameter sets) are queued in
+   arrival order and admitted while a slot is free and the device memory the
+   admitted requests hold (ccf_estimate_device_bytes, counted from admission
+   until ccf_server_release) stays within hbm_budget.  Each admitted request
+   runs on its own handle, engine and CUDA stream, so the work of concurrent
+   requests overlaps on the device; its stars, tree, roots and results stay
+   resident until released.  A request larger than the whole budget is
+   rejected (CCF_ERR_BUDGET); one that had to wait at the head of the queue
+   for memory is counted as deferred.  No reference counterpart: the
+   reference resets the device on every run (include/ccf.cuh:151). */
+typedef struct ccf_server ccf_server;
+
+typedef struct ccf_server_config
+{
+	int device;                    /* CUDA device ordinal */
+	int slots;                     /* requests running at once (>= 1) */
+	unsigned long long hbm_budget; /* bytes admitted requests may hold */
+	int verbose;                   /* passed to each run */
+	int reserved[7];
+} ccf_server_config;
+
+typedef enum ccf_request_state
+{
+	CCF_REQUEST_QUEUED = 0,
+	CCF_REQUEST_RUNNING = 1,
+	CCF_REQUEST_DONE = 2,
+	CCF_REQUEST_FAILED = 3,
+	CCF_REQUEST_REJECTED = 4
+} ccf_request_state;
+
+typedef struct ccf_request_info
+{
+	int state;                 /* ccf_request_state */
+	int status;                /* ccf_status of the run once done, failed or rejected */
+	int deferred;              /* 1 if it waited at the head of the queue for memory */
+	int reserved0;
+	unsigned long long bytes;  /* admission estimate */
+	double t_submit;           /* seconds since the server was created */
+	double t_start;
+	double t_end;
+	double reserved[4];
+} ccf_request_info;
+
+typedef struct ccf_server_stats
+{
+	long long submitted, admitted, completed, failed, rejected, deferred, queued, running;
+	unsigned long long bytes_in_use, hbm_budget;
+	double reserved[4];
+} ccf_server_stats;
+
+ccf_status ccf_server_create(const ccf_server_config* cfg, ccf_server** out);
+/* queue a request; *id identifies it in the calls below */
+ccf_status ccf_server_submit(ccf_server* s, const ccf_params* p, long long* id);
+/* wait until the request is done, failed or rejected (timeout_seconds < 0:
+   no limit); CCF_ERR_TIMEOUT if it is still queued or running */
+ccf_status ccf_server_wait(ccf_server* s, long long id, double timeout_seconds);
+ccf_status ccf_server_request_info(ccf_server* s, long long id, ccf_request_info* out);
+/* the handle holding a finished request's field and results (owned by the
+   server until ccf_server_release; use ccf_get_results, ccf_get_info,
+   ccf_save, ccf_last_error on it) */
+ccf_status ccf_server_handle(ccf_server* s, long long id, ccf_handle** h);
+/* free a finished request's device memory and return it to the budget */
+ccf_status ccf_server_release(ccf_server* s, long long id);
+ccf_status ccf_server_get_stats(ccf_server* s, ccf_server_stats* out);
+/* waits for running requests, drops queued ones, frees everything */
+void ccf_server_destroy(ccf_server* s);
+
 #ifdef __cplusplus
 }
 #endif
