@@ -53,6 +53,64 @@ WORKLOADS = {
         num_branches=128, random_seed=1236),
 }
 DEFAULT = "single_field_n2000_salpeter_rect"
+# workloads of many fields: a step is one pass over the whole set
+MULTI_WORKLOADS = ("batch_256_fields_n50_1000_disc", "serving_poisson_salpeter_disc")
+
+
+def _singular(kappa: float, shear: float) -> bool:
+    """|1 - kappa| or |1 - kappa -/+ shear| near 0 blows up the field size."""
+    return abs(1 - kappa) < 0.05 or abs(1 - kappa - shear) < 0.05 or abs(1 - kappa + shear) < 0.05
+
+
+def batch_fields(count: int = 256) -> list[dict]:
+    """256 independent disc fields of equal masses: N ~ U{50..1000}, kappa_star
+    ~ U[0.05, 0.6], smooth fraction s ~ U[0, 0.3] (kappa_tot = kappa_star /
+    (1 - s)), shear ~ U[0, 0.5], rejecting near-singular (kappa_tot, shear);
+    num_phi 512 (the nearest value the reference accepts for 500: a multiple
+    of 2 * num_branches), 8 branches, star seeds 10000 + i."""
+    import numpy as np
+    rng = np.random.default_rng(2024)
+    out = []
+    while len(out) < count:
+        n = int(rng.integers(50, 1001))
+        ks = float(rng.uniform(0.05, 0.6))
+        s = float(rng.uniform(0.0, 0.3))
+        g = float(rng.uniform(0.0, 0.5))
+        k = ks / (1 - s)
+        if _singular(k, g):
+            continue
+        out.append(dict(kappa_tot=k, kappa_star=ks, shear=g, theta_star=1.0, mass_function="equal", rectangular=0,
+                        approx=1, num_stars=n, num_phi=512, num_branches=8, random_seed=10000 + len(out)))
+    return out
+
+
+def serving_requests(count: int) -> list[tuple[float, dict]]:
+    """Poisson request stream (exponential inter-arrival times, mean 50 ms,
+    seed 4242): N log-uniform in [100, 50000], kappa_star ~ U[0.1, 0.8]
+    (kappa_tot = kappa_star), shear ~ U[0, 0.6] rejecting near-singular
+    values, Salpeter masses on [0.08, 1.5] with mean 1, discs,
+    num_branches in {8, 32, 128}, num_phi = 2 nb ceil(U[1000, 10000] / 2 nb),
+    star seeds 20000 + i.  Returns (arrival time in s, parameters)."""
+    import math
+    import numpy as np
+    rng = np.random.default_rng(4242)
+    t = 0.0
+    out = []
+    while len(out) < count:
+        ks = float(rng.uniform(0.1, 0.8))
+        g = float(rng.uniform(0.0, 0.6))
+        if _singular(ks, g):
+            continue
+        n = int(round(math.exp(rng.uniform(math.log(100), math.log(50000)))))
+        nb = int(rng.choice([8, 32, 128]))
+        nphi = 2 * nb * int(math.ceil(rng.uniform(1000, 10000) / (2 * nb)))
+        t += float(rng.exponential(0.05))
+        out.append((t, dict(kappa_tot=ks, kappa_star=ks, shear=g, theta_star=1.0, mass_function="salpeter",
+                            m_lower=0.08, m_upper=1.5, m_solar=4.954984, rectangular=0, approx=1, num_stars=n,
+                            num_phi=nphi, num_branches=nb, random_seed=20000 + len(out))))
+    return out
+
+
 METRIC = "crit-curve pts/s mixed vs plain FP64 (err≤1e-9); fields/s, p50/p99 latency"
 
 
@@ -180,6 +238,166 @@ def cpu_reference(cfg: dict, threads: int, branches: int | None = None, steps: i
             "cores": threads}
 
 
+def run_multi(args) -> None:
+    """Workloads of many fields.  batch: one run_batch over 256 fields per
+    step.  serving: a Poisson stream of requests through the request loop
+    (ccf_server_*), timed from the first arrival to the last completion, with
+    queue-inclusive latencies."""
+    ws, rank, local = dist_env()
+    import numpy as np
+    import torch
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from ccf_gb300 import CCF, Server, run_batch
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+
+    def reduce(x: float, op) -> float:
+        if ws == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=op)
+        return float(t.item())
+
+    MAX = SUM = None
+    if ws > 1:
+        MAX, SUM = torch.distributed.ReduceOp.MAX, torch.distributed.ReduceOp.SUM
+
+    line = {"metric": METRIC, "unit": "points/s", "n_gpus": ws, "steps": args.steps, "warmup": max(3, args.warmup),
+            "higher_is_better": True, "vs_baseline": None, "data": "synthetic (seeded star fields)",
+            "dtype": "f32+df32+f64 (FP32 correction sums, double-float f and caustics, FP64 off the corner circle)"}
+    with ClockSampler(local) as clocks:
+        if args.workload == "batch_256_fields_n50_1000_disc":
+            fields = batch_fields()
+            mine = fields[rank::ws]           # the fields are independent: split them between ranks
+
+            def make(prec):
+                cs = []
+                for f in mine:
+                    c = CCF(**f)
+                    c.precision, c.device, c.write_mu_length_scales = prec, local, 0
+                    cs.append(c)
+                return cs
+
+            def one_pass(cs, results=False):
+                barrier()
+                t0 = time.perf_counter()
+                assert run_batch(cs), cs[0].last_error()
+                out = [c.results(stars=False) for c in cs] if results else None
+                barrier()
+                return time.perf_counter() - t0, out
+
+            cs = make("mixed")
+            for _ in range(max(3, args.warmup)):
+                one_pass(cs)
+            ts = [one_pass(cs)[0] for _ in range(args.steps)]
+            t = reduce(statistics.median(ts), MAX)
+            pts = reduce(float(sum(c.info()["num_points"] for c in cs)), SUM)
+            te, outs = one_pass(cs, results=True)
+            te = reduce(te, MAX)
+            d2h = sum(o["ccs"].nbytes + o["caustics"].nbytes + o["errs"].nbytes for o in outs)
+            fp = make("fp64")
+            one_pass(fp)
+            t64 = reduce(one_pass(fp)[0], MAX)
+            line.update({"value": pts / t, "ms_per_step": 1e3 * t, "scaling": "strong",
+                         "fields_per_s": len(fields) / t,
+                         "config": {"workload": args.workload, "fields": len(fields), "num_phi": 512,
+                                    "num_branches": 8, "num_stars": "U{50..1000}", "mass_function": "equal",
+                                    "geometry": "disc", "precision": "mixed",
+                                    "l2": "inputs are 256 fields; no flush between passes",
+                                    "parallelism": f"fields split over {ws} GPU(s)"},
+                         "e2e": {"value": pts / te, "unit": "points/s", "h2d_bytes_per_step": 0,
+                                 "d2h_bytes_per_step": d2h},
+                         "fp64_plain": {"value": pts / t64, "unit": "points/s", "ms_per_step": 1e3 * t64},
+                         "gpu_launches": 2 + int(sum(c.info()["kernel_launches"] - 2 for c in cs)),
+                         "detail": {"points": pts, "max_error_1/mu": max(c.info()["max_error"] for c in cs),
+                                    "unconverged": int(sum(c.info()["unconverged"] for c in cs))}})
+            if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+                threads = os.cpu_count() or 1
+                tc, pc = 0.0, 0.0
+                for f in fields[:16]:
+                    cb = cpu_reference(f, threads, steps=2)
+                    tc += cb["t_full_extrapolated"]
+                    pc += cb["value"] * cb["t_full_extrapolated"]
+                line["cpu_baseline"] = {"value": pc / tc, "unit": "points/s", "cores": threads, "kind": "port",
+                                        "sample": "the first 16 of the 256 fields, each on all branches and 2 phi "
+                                                  "steps per side, extrapolated in steps"}
+        else:
+            reqs = serving_requests(args.requests)[rank::ws]
+
+            def stream(prec, requests):
+                s = Server(slots=args.slots, hbm_budget=args.hbm_budget, device=local)
+                ids = []
+                t0 = time.perf_counter()
+
+                def submitter():
+                    for t_arr, p in requests:
+                        dt = t0 + t_arr - time.perf_counter()
+                        if dt > 0:
+                            time.sleep(dt)
+                        ids.append(s.submit(precision=prec, write_mu_length_scales=0, write_stars=0, **p))
+
+                th = threading.Thread(target=submitter)
+                th.start()
+                infos, pts, failed = [], 0, 0
+                k = 0
+                while k < len(requests):
+                    if k >= len(ids):
+                        time.sleep(0.001)
+                        continue
+                    rid = ids[k]
+                    st = s.wait(rid)
+                    infos.append(s.info(rid))
+                    if st == 0:
+                        pts += s.field(rid).info()["num_points"]
+                    else:
+                        failed += 1
+                    s.release(rid)
+                    k += 1
+                th.join()
+                stats = s.stats()
+                s.close()
+                span = max(i["t_end"] for i in infos) - min(i["t_submit"] for i in infos)
+                lat = sorted(i["t_end"] - i["t_submit"] for i in infos)
+                return {"points": pts, "span": span, "latency": lat, "stats": stats, "failed": failed}
+
+            stream("mixed", [(0.0, p) for _, p in serving_requests(4)])   # warm-up
+            r = stream("mixed", reqs)
+            span = reduce(r["span"], MAX)
+            pts = reduce(float(r["points"]), SUM)
+            lat = r["latency"]
+            sub = reqs[:args.fp64_requests]
+            r64 = stream("fp64", sub)
+            rm = stream("mixed", sub)
+            line.update({"value": pts / span, "ms_per_step": 1e3 * span, "steps": 1, "scaling": "weak",
+                         "fields_per_s": reduce(float(len(reqs)), SUM) / span,
+                         "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
+                         "config": {"workload": args.workload, "requests": args.requests, "slots": args.slots,
+                                    "hbm_budget_bytes": args.hbm_budget, "arrivals": "Poisson, mean 50 ms, seed 4242",
+                                    "num_stars": "log-uniform [100, 50000]", "num_branches": "{8, 32, 128}",
+                                    "num_phi": "2 nb ceil(U[1000, 10000] / 2 nb)", "mass_function": "salpeter",
+                                    "geometry": "disc", "precision": "mixed", "l2": "inputs are whole fields; no flush",
+                                    "parallelism": f"request streams split over {ws} GPU(s)"},
+                         "e2e": {"value": pts / span, "unit": "points/s", "h2d_bytes_per_step": 0,
+                                 "d2h_bytes_per_step": 0},
+                         "server": dict(r["stats"]),
+                         "fp64_plain": {"requests": len(sub), "value": r64["points"] / r64["span"],
+                                        "mixed_same_requests": rm["points"] / rm["span"], "unit": "points/s",
+                                        "ratio_mixed_over_fp64": (rm["points"] / rm["span"]) / (r64["points"] / r64["span"])},
+                         "gpu_launches": None,
+                         "detail": {"points": pts, "failed": r["failed"]}})
+    line["clocks"] = clocks.summary()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
 def run_reference(args) -> None:
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -211,13 +429,20 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default=DEFAULT, choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default=DEFAULT, choices=sorted(WORKLOADS) + list(MULTI_WORKLOADS))
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--fp64-steps", type=int, default=1, help="plain-FP64 steps timed beside the main arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--requests", type=int, default=64, help="serving: requests in the stream")
+    ap.add_argument("--slots", type=int, default=4, help="serving: requests running at once")
+    ap.add_argument("--hbm-budget", type=float, default=60e9, help="serving: admission budget in bytes")
+    ap.add_argument("--fp64-requests", type=int, default=6, help="serving: requests replayed in plain FP64")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload in MULTI_WORKLOADS:
+        run_multi(args)
         return
 
     ws, rank, local = dist_env()
@@ -300,7 +525,25 @@ def main() -> None:
     hbm_peak = hbm_peak_gbs()
 
     fp64 = None
-    if args.precision == "mixed" and args.fp64_steps > 0:
+    if args.precision == "mixed" and args.fp64_steps > 0 and cfg["num_stars"] > 5000:
+        # a plain-FP64 run of a field this large takes minutes: time both
+        # precisions on the same field with 2 phi steps per side and apply
+        # their ratio to the full mixed run
+        red = dict(cfg, num_phi=4 * cfg["num_branches"])
+        tm, td = [], []
+        for prec, acc in (("mixed", tm), ("fp64", td)):
+            c2 = CCF(**red)
+            c2.precision, c2.device, c2.write_mu_length_scales = prec, local, 0
+            for _ in range(1 + args.fp64_steps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                assert c2.run(-1), c2.last_error()
+                acc.append(c2.info()["t_total"])
+        ratio = statistics.median(td[1:]) / statistics.median(tm[1:])
+        fp64 = {"value": value / ratio, "unit": "points/s", "ms_per_step": 1e3 * t_dev / args.steps * ratio,
+                "extrapolated": f"fp64/mixed time ratio {ratio:.2f} measured on the same field with num_phi "
+                                f"{red['num_phi']} (2 phi steps per side), applied to the full mixed run"}
+    elif args.precision == "mixed" and args.fp64_steps > 0:
         d = make("fp64")
         assert d.run(-1), d.last_error()
         tt = []
@@ -315,7 +558,8 @@ def main() -> None:
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        cb = cpu_reference(cfg, threads, steps=2)
+        # large fields: the initial solve and 2 phi steps of 4 branches
+        cb = cpu_reference(cfg, threads, branches=4 if cfg["num_stars"] > 5000 else None, steps=2)
         cpu = {"value": cb["value"], "unit": "points/s", "cores": threads, "kind": "port", "sample": cb["sample"]}
 
     if rank == 0:
