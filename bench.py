@@ -111,6 +111,29 @@ def serving_requests(count: int) -> list[tuple[float, dict]]:
     return out
 
 
+def reduce_over_ranks(x: float, op: str, ws: int, device: str = "cuda") -> float:
+    """Max or sum of a scalar over the ranks of the process group (the
+    slowest replica's time, all replicas' points); the identity on one rank.
+    The only collective of a multi-GPU run: replicas share no data."""
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op={"max": dist.ReduceOp.MAX, "sum": dist.ReduceOp.SUM}[op])
+    return float(t.item())
+
+
+def shard(items: list, rank: int, ws: int) -> list:
+    """The independent units (fields, requests) rank takes: every ws-th one."""
+    return items[rank::ws]
+
+
+def replica_seed(seed: int, rank: int) -> int:
+    """Star seed of rank's replica of the single-field workload."""
+    return seed + rank
+
+
 METRIC = "crit-curve pts/s mixed vs plain FP64 (err≤1e-9); fields/s, p50/p99 latency"
 
 
@@ -257,16 +280,10 @@ def run_multi(args) -> None:
         if ws > 1:
             torch.distributed.barrier()
 
-    def reduce(x: float, op) -> float:
-        if ws == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=op)
-        return float(t.item())
+    def reduce(x: float, op: str) -> float:
+        return reduce_over_ranks(x, op, ws)
 
-    MAX = SUM = None
-    if ws > 1:
-        MAX, SUM = torch.distributed.ReduceOp.MAX, torch.distributed.ReduceOp.SUM
+    MAX, SUM = "max", "sum"
 
     line = {"metric": METRIC, "unit": "points/s", "n_gpus": ws, "steps": args.steps, "warmup": max(3, args.warmup),
             "higher_is_better": True, "vs_baseline": None, "data": "synthetic (seeded star fields)",
@@ -274,7 +291,7 @@ def run_multi(args) -> None:
     with ClockSampler(local) as clocks:
         if args.workload == "batch_256_fields_n50_1000_disc":
             fields = batch_fields()
-            mine = fields[rank::ws]           # the fields are independent: split them between ranks
+            mine = shard(fields, rank, ws)    # the fields are independent: split them between ranks
 
             def make(prec):
                 cs = []
@@ -328,7 +345,7 @@ def run_multi(args) -> None:
                                         "sample": "the first 16 of the 256 fields, each on all branches and 2 phi "
                                                   "steps per side, extrapolated in steps"}
         else:
-            reqs = serving_requests(args.requests)[rank::ws]
+            reqs = shard(serving_requests(args.requests), rank, ws)
 
             def stream(prec, requests):
                 s = Server(slots=args.slots, hbm_budget=args.hbm_budget, device=local)
@@ -455,7 +472,7 @@ def main() -> None:
     from ccf_gb300 import CCF
 
     cfg = dict(WORKLOADS[args.workload])
-    cfg["random_seed"] = cfg["random_seed"] + rank
+    cfg["random_seed"] = replica_seed(cfg["random_seed"], rank)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     def make(prec):
@@ -484,11 +501,7 @@ def main() -> None:
             assert c.run(-1), c.last_error()
             infos.append(c.info())
         barrier()
-    t_dev = sum(i["t_total"] for i in infos)
-    if ws > 1:
-        t = torch.tensor([t_dev], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_dev = float(t.item())
+    t_dev = reduce_over_ranks(sum(i["t_total"] for i in infos), "max", ws)
     info = infos[-1]
     points = info["num_points"]
     value = points * args.steps * ws / t_dev
