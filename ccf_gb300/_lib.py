@@ -21,6 +21,8 @@ STATUS_NAMES = {
 STATUS_CODES = {name: code for code, name in STATUS_NAMES.items()}
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
+CONTINUATION_TRACK = 0
+CONTINUATION_ABERTH = 1
 
 
 class CcfParams(ctypes.Structure):
@@ -52,7 +54,8 @@ class CcfParams(ctypes.Structure):
         ("max_iters_step", ctypes.c_int),
         ("exact_binomials", ctypes.c_int),
         ("device", ctypes.c_int),
-        ("reserved", ctypes.c_int * 8),
+        ("continuation", ctypes.c_int),
+        ("reserved", ctypes.c_int * 7),
     ]
 
 
@@ -102,7 +105,10 @@ class CcfInfo(ctypes.Structure):
         ("kernel_launches", ctypes.c_longlong),
         ("root_updates_init", ctypes.c_longlong),
         ("sum_terms_init", ctypes.c_longlong),
-        ("reserved", ctypes.c_double * 5),
+        ("rows_rerun", ctypes.c_longlong),
+        ("step_halvings", ctypes.c_longlong),
+        ("rerun_flags", ctypes.c_longlong),
+        ("reserved", ctypes.c_double * 2),
     ]
 
     def as_dict(self) -> dict:

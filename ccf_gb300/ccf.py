@@ -66,6 +66,7 @@ class CCF:
         self.max_iters_step = 60
         self.exact_binomials = 0
         self.device = 0
+        self.continuation = "track"
         self._stars_keep = None
         self.last_status = 0
         for k, v in kw.items():
@@ -101,6 +102,7 @@ class CCF:
         p.max_iters_step = int(self.max_iters_step)
         p.exact_binomials = int(self.exact_binomials)
         p.device = int(self.device)
+        p.continuation = _continuation_code(self.continuation)
         return p
 
     def _push(self):
@@ -249,6 +251,17 @@ def submit_batch(fields: list[CCF], verbose: int = 0) -> BatchJob:
     return BatchJob(fields, verbose)
 
 
+def _continuation_code(v) -> int:
+    """'track' (per-root tracking, checked, with the full-sum re-run) or
+    'aberth' (the full Aberth step of the reference for every root)."""
+    k = str(v).lower()
+    if k in ("track", "0"):
+        return _lib.CONTINUATION_TRACK
+    if k in ("aberth", "1"):
+        return _lib.CONTINUATION_ABERTH
+    raise ValueError(f"continuation must be 'track' or 'aberth', not {v!r}")
+
+
 def _bare(**kw) -> CCF:
     """A CCF parameter holder without a native handle."""
     c = CCF.__new__(CCF)
@@ -259,6 +272,7 @@ def _bare(**kw) -> CCF:
         setattr(c, k, v)
     c.precision, c.output_float, c.max_iters_init, c.max_iters_step, c.exact_binomials, c.device = \
         "mixed", 0, 300, 60, 0, 0
+    c.continuation = "track"
     c._stars_keep = None
     c.last_status = 0
     for k, v in kw.items():

@@ -63,6 +63,7 @@ void ccf_default_params(ccf_params* p)
 	p->max_iters_step = 60;
 	p->exact_binomials = 0;
 	p->device = 0;
+	p->continuation = CCF_CONTINUATION_TRACK;
 }
 
 ccf_status ccf_create(ccf_handle** out)

@@ -1,8 +1,9 @@
 /******************************************************************************
 cli.cpp -- ccf_gpu, the command line of the reference's main_ccf
 (src/main_ccf.cu) over the C ABI: the same 24 option pairs with the same
-meanings, defaults, messages and exit codes, plus two additive options,
--pr/--precision (mixed or fp64) and -d/--device.
+meanings, defaults, messages and exit codes, plus three additive options,
+-pr/--precision (mixed or fp64), -ct/--continuation (track or aberth) and
+-d/--device.
 ******************************************************************************/
 #include "ccf_gb300.hpp"
 
@@ -15,14 +16,14 @@ meanings, defaults, messages and exit codes, plus two additive options,
 namespace
 {
 
-/* src/main_ccf.cu:29-56, plus the two additions */
+/* src/main_ccf.cu:29-56, plus the three additions */
 const std::vector<std::string> OPTS = {
 	"-h", "--help", "-v", "--verbose", "-k", "--kappa_tot", "-y", "--shear", "-s", "--smooth_fraction",
 	"-ks", "--kappa_star", "-t", "--theta_star", "-mf", "--mass_function", "-ms", "--m_solar",
 	"-ml", "--m_lower", "-mh", "--m_upper", "-r", "--rectangular", "-a", "--approx", "-ss", "--safety_scale",
 	"-ns", "--num_stars", "-sf", "--starfile", "-np", "--num_phi", "-nb", "--num_branches",
 	"-rs", "--random_seed", "-ws", "--write_stars", "-wcc", "--write_critical_curves", "-wc", "--write_caustics",
-	"-wls", "--write_length_scales", "-o", "--outfile_prefix", "-pr", "--precision", "-d", "--device"};
+	"-wls", "--write_length_scales", "-o", "--outfile_prefix", "-pr", "--precision", "-ct", "--continuation", "-d", "--device"};
 
 bool exists(char** b, char** e, const std::string& o) { return std::find(b, e, o) != e; }
 
@@ -116,6 +117,10 @@ static void display_usage(char* name)
 		<< "  -pr,--precision            Root solver arithmetic: mixed (FP32 correction sums,\n"
 		<< "                             double-float critical-curve function) or fp64.\n"
 		<< "                             Default value: mixed\n"
+		<< "  -ct,--continuation         Phi continuation: track (each root on its own,\n"
+		<< "                             checked, full-sum re-run of failing rows) or\n"
+		<< "                             aberth (full Aberth step for every root).\n"
+		<< "                             Default value: track\n"
 		<< "  -d,--device                CUDA device ordinal. Default value: 0\n";
 }
 
@@ -206,6 +211,12 @@ int main(int argc, char* argv[])
 				std::string pr = lower(in);
 				if (pr != "mixed" && pr != "fp64") throw std::invalid_argument("precision");
 				set_param("precision", ccf.precision, pr == "mixed" ? CCF_PRECISION_MIXED : CCF_PRECISION_FP64, verbose);
+			}
+			else if (is("-ct", "--continuation"))
+			{
+				std::string ct = lower(in);
+				if (ct != "track" && ct != "aberth") throw std::invalid_argument("continuation");
+				set_param("continuation", ccf.continuation, ct == "track" ? CCF_CONTINUATION_TRACK : CCF_CONTINUATION_ABERTH, verbose);
 			}
 			else if (is("-d", "--device")) set_param("device", ccf.device, std::stoi(in), verbose);
 		}

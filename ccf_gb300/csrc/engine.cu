@@ -508,16 +508,29 @@ ccf_status Engine::build_fmm(Field& f)
 	return CCF_OK;
 }
 
+static size_t nb_total(const std::vector<Field*>& fields)
+{
+	size_t n = 0;
+	for (const Field* f : fields) n += (size_t)f->params.num_branches;
+	return n;
+}
+
 ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 {
 	cudaStream_t s = stream;
 	const int nf = (int)fields.size();
 	const bool mixed = fields[0]->params.precision == CCF_PRECISION_MIXED;
+	const bool track = fields[0]->params.continuation == CCF_CONTINUATION_TRACK;
 	for (Field* f : fields)
 	{
 		if ((f->params.precision == CCF_PRECISION_MIXED) != mixed)
 		{
 			error = "Error. All fields of a batch must use the same precision.";
+			return CCF_ERR_INVALID_ARGUMENT;
+		}
+		if ((f->params.continuation == CCF_CONTINUATION_TRACK) != track)
+		{
+			error = "Error. All fields of a batch must use the same continuation.";
 			return CCF_ERR_INVALID_ARGUMENT;
 		}
 	}
@@ -560,6 +573,8 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 	std::vector<const float4*> hilo(nf);
 	std::vector<RowDesc> ri, rc;
 	std::vector<double> cost_i, cost_c;
+	long long table_slots = 0;   /* tracker: 2 R slots per phi step of every continuation row */
+	std::vector<int> item_start_host(2 * nb_total(fields));
 	for (int i = 0; i < nf; i++)
 	{
 		Field& f = *fields[i];
@@ -601,7 +616,8 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 				RowDesc q = r;
 				q.side = b;
 				q.base = cont_off[i] + (long long)(2 * c + b) * R;
-				q.cont_base = 0;
+				q.cont_base = table_slots;
+				table_slots += 2LL * R * (o.step_last - o.step_first + 1);
 				rc.push_back(q);
 				cost_c.push_back(cost * o.half);
 			}
@@ -633,6 +649,14 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 	CCF_TRY(cudaMemcpyAsync(P.rows_init.ptr, ri.data(), ri.size() * sizeof(RowDesc), cudaMemcpyHostToDevice, s), "upload");
 	CCF_TRY(cudaMemcpyAsync(P.rows_cont.ptr, rc.data(), rc.size() * sizeof(RowDesc), cudaMemcpyHostToDevice, s), "upload");
 	CCF_TRY(cudaMemsetAsync(P.error.ptr, 0, sizeof(int), s), "memset");
+	if (track)
+	{
+		CCF_TRY(P.track_table.ensure(table_slots), "cudaMalloc(tables)");
+		CCF_TRY(P.row_stats.ensure(3 * rc.size()), "cudaMalloc(rows)");
+		CCF_TRY(P.rows_rerun.ensure(rc.size()), "cudaMalloc(rows)");
+		CCF_TRY(P.rerun_count.ensure(2), "cudaMalloc(rows)");
+		CCF_TRY(P.item_start.ensure(rc.size()), "cudaMalloc(rows)");
+	}
 
 	/* CTAs per row: fill the resident slots without a second wave */
 	const int slots = num_sms * slots_per_sm;
@@ -671,6 +695,36 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 	A.fin = P.fin_cont.ptr;
 	A.list = P.list_cont.ptr;
 	A.fval = P.fval_cont.ptr;
+	if (track)
+	{
+		/* every root on its own path; rows that fail the column check run
+		   again from their branch-centre roots with the full Aberth step */
+		TrackArgs T;
+		T.fields = P.views.ptr;
+		T.outs = P.outs.ptr;
+		T.rows = P.rows_cont.ptr;
+		T.num_rows = (int)rc.size();
+		T.master = P.master_cont.ptr;
+		T.table = P.track_table.ptr;
+		T.row_stats = P.row_stats.ptr;
+		T.item_start = P.item_start.ptr;
+		T.counter = P.rerun_count.ptr + 1;
+		T.num_items = 0;
+		for (size_t r = 0; r < rc.size(); r++)
+		{
+			item_start_host[r] = T.num_items;
+			T.num_items += (fields[rc[r].field]->d.num_roots + 31) / 32;
+		}
+		CCF_TRY(cudaMemcpyAsync(P.item_start.ptr, item_start_host.data(), rc.size() * sizeof(int), cudaMemcpyHostToDevice, s),
+			"upload");
+		CCF_TRY(cudaMemsetAsync(P.track_table.ptr, 0, table_slots * sizeof(unsigned long long), s), "memset");
+		CCF_TRY(cudaMemsetAsync(P.row_stats.ptr, 0, 3 * rc.size() * sizeof(unsigned long long), s), "memset");
+		CCF_TRY(cudaMemsetAsync(P.rerun_count.ptr, 0, 2 * sizeof(int), s), "memset");
+		CCF_TRY(launch_track(s, T, mixed), "track_ccs");
+		CCF_TRY(launch_collect_rerun(s, T, P.rows_rerun.ptr, P.rerun_count.ptr), "collect_rerun");
+		A.rows = P.rows_rerun.ptr;
+		A.num_rows_dev = P.rerun_count.ptr;
+	}
 	CCF_TRY(launch_solve(s, A, mixed, false), "find_ccs");
 	for (Field* f : fields) CCF_TRY(cudaEventRecord(f->ev[5], s), "event");
 	CCF_TRY(cudaStreamSynchronize(s), "solver");
@@ -692,13 +746,18 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		info.max_sweeps_step = (int)st[6];
 		info.root_updates_init = (long long)st[7];
 		info.sum_terms_init = (long long)st[8];
+		info.rows_rerun = (long long)st[9];
+		info.step_halvings = (long long)st[10];
+		info.rerun_flags = (long long)st[11];
 		info.t_stars = ev_ms(f->ev[0], f->ev[1]) * 1e-3;
 		info.t_tree = ev_ms(f->ev[1], f->ev[2]) * 1e-3;
 		info.t_init_roots = ev_ms(f->ev[3], f->ev[4]) * 1e-3;
 		info.t_ccs = ev_ms(f->ev[4], f->ev[5]) * 1e-3;
 		info.t_caustics = 0;
 		info.t_total = ev_ms(f->ev[0], f->ev[5]) * 1e-3;
-		info.kernel_launches += 3;   /* root seeds, initial solve, continuation */
+		/* root seeds, initial solve, continuation (tracker: tracking, row
+		   collection and the full-sum launch for the rows to re-run) */
+		info.kernel_launches += track ? 5 : 3;
 		if (info.has_nan)
 		{
 			f->error = "Error. Errors in 1/mu contain values which are not positive real numbers.";

@@ -118,7 +118,7 @@ struct Field
 	/* outputs, file layout */
 	DBuf<double2> ccs, caustics;
 	DBuf<double> errs, mu;
-	DBuf<unsigned long long> stats;   /* solver statistics, 8 words */
+	DBuf<unsigned long long> stats;   /* solver statistics, 16 words (kernels.h, FieldOut::stats) */
 
 	/* timing */
 	cudaEvent_t ev[8] = {};
@@ -136,7 +136,11 @@ struct SolverPools
 	DBuf<unsigned char> fin_init, fin_cont;
 	DBuf<int> list_init, list_cont;
 	DBuf<double2> fval_init, fval_cont;   /* f, f' per root */
-	DBuf<RowDesc> rows_init, rows_cont;
+	DBuf<RowDesc> rows_init, rows_cont, rows_rerun;
+	DBuf<unsigned long long> track_table;   /* column tables of the tracker */
+	DBuf<unsigned long long> row_stats;     /* 3 per continuation row */
+	DBuf<int> rerun_count;                  /* [0] rows to re-run, [1] tracker work counter */
+	DBuf<int> item_start;                   /* first tracker work item of each continuation row */
 	DBuf<FieldView> views;
 	DBuf<FieldOut> outs;
 	DBuf<const float4*> hilo_ptrs;

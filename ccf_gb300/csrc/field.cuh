@@ -389,6 +389,25 @@ CCF_D bool smooth_df_ok(const FieldView& F, double2 z)
 	return z.x * z.x + z.y * z.y < SMOOTH_DF_RANGE * F.corner_abs * F.corner_abs;
 }
 
+/* d2 alpha_smooth / d zbar2 in FP32 (the FP32 Taylor polynomial within the
+   corner circle, FP64 outside) */
+CCF_D float2 smooth_d2zbar_f32(const FieldView& F, double2 z)
+{
+	if (F.rectangular && F.approx && F.smooth_m > 0 && smooth_df_ok(F, z))
+	{
+		double2 zb = cconj(z);
+		double2 rd = cmul(zb, F.inv_corner);
+		float2 r = make_float2((float)rd.x, (float)rd.y);
+		float2 u = fmulc(r, r);
+		float2 acc = F.smooth_d2f[F.smooth_m - 1];
+		for (int m = F.smooth_m - 2; m >= 0; m--) acc = fadd(fmulc(acc, u), F.smooth_d2f[m]);
+		double2 pre = cmul(zb, F.inv_corner2);
+		return fmulc(acc, make_float2((float)pre.x, (float)pre.y));
+	}
+	double2 t = smooth_d2zbar(F, z);
+	return make_float2((float)t.x, (float)t.y);
+}
+
 /* f'(z) in FP32 for the mixed-precision solver: only the step size depends
    on it, never the converged root.  Off-field points take s3_off, the direct
    sum over every star. */
@@ -423,23 +442,7 @@ CCF_D float2 eval_df32(const FieldView& F, int leaf, double2 z, double2 s3_off)
 	{
 		s3 = make_float2((float)s3_off.x, (float)s3_off.y);
 	}
-	float2 d2s;
-	if (F.rectangular && F.approx && F.smooth_m > 0 && smooth_df_ok(F, z))
-	{
-		double2 zb = cconj(z);
-		double2 rd = cmul(zb, F.inv_corner);
-		float2 r = make_float2((float)rd.x, (float)rd.y);
-		float2 u = fmulc(r, r);
-		float2 acc = F.smooth_d2f[F.smooth_m - 1];
-		for (int m = F.smooth_m - 2; m >= 0; m--) acc = fadd(fmulc(acc, u), F.smooth_d2f[m]);
-		double2 pre = cmul(zb, F.inv_corner2);
-		d2s = fmulc(acc, make_float2((float)pre.x, (float)pre.y));
-	}
-	else
-	{
-		double2 t = smooth_d2zbar(F, z);
-		d2s = make_float2((float)t.x, (float)t.y);
-	}
+	const float2 d2s = smooth_d2zbar_f32(F, z);
 	const float t2 = (float)F.theta2;
 	return make_float2(-2 * t2 * s3.x - d2l.x - d2s.x, -2 * t2 * s3.y - d2l.y + d2s.y);
 }

@@ -188,6 +188,72 @@ CCF_D double2 eval_f_df(const FieldView& F, int leaf, double2 z, double cphi, do
 	return f;
 }
 
+/* What one corrector iteration of the continuation tracker needs at a root
+   inside the root box: f (double-float, as eval_f_df), f' (FP32, as
+   eval_df32) and the pole sum 2 sum_i 1/(z - z_i) over the leaf's near stars
+   (FP32), from one pass over those stars: the FP32 terms are the high words
+   of the double-float 1/d and 1/d^2 the pass forms for f.  rel = z - leaf
+   centre in FP64. */
+struct TrackEval
+{
+	double2 f;
+	float2 df;
+	float2 pole;
+};
+
+CCF_D TrackEval eval_track_df(const FieldView& F, int leaf, double2 z, double2 rel, double cphi, double sphi)
+{
+	const dfc zr = dfc_from(rel);
+	dfc s2 = {{0.f, 0.f}, {0.f, 0.f}};
+	float2 s3 = make_float2(0.f, 0.f), pole = make_float2(0.f, 0.f);
+	const int n = F.leaf_near_count[leaf];
+	const float4* Pn = F.leaf_near_df + (size_t)leaf * MAX_NEAR;
+	const float2* Mn = F.leaf_mass_df + (size_t)leaf * MAX_NEAR;
+	for (int i = 0; i < n; i++)
+	{
+		const dfc s = dfc_load(Pn[i]);
+		const float2 mm = Mn[i];
+		const dfl m = {mm.x, mm.y};
+		const dfl dx = df_sub(zr.re, s.re);
+		const dfl dy = df_sub(zr.im, s.im);
+		const dfl r = df_rcp(df_add_fast(df_sqr(dx), df_sqr(dy)));
+		const dfl ix = df_mul(dx, r);
+		const dfl iy = df_neg(df_mul(dy, r));                     /* 1/d */
+		const dfl i2x = df_add(df_sqr(ix), df_neg(df_sqr(iy)));
+		dfl i2y = df_mul(ix, iy);
+		i2y = {2.f * i2y.hi, 2.f * i2y.lo};                        /* 1/d^2 */
+		s2.re = df_add_fast(s2.re, df_mul(m, i2x));
+		s2.im = df_add_fast(s2.im, df_mul(m, i2y));
+		pole.x += ix.hi;
+		pole.y += iy.hi;
+		const float i3x = i2x.hi * ix.hi - i2y.hi * iy.hi;
+		const float i3y = i2x.hi * iy.hi + i2y.hi * ix.hi;        /* 1/d^3 */
+		s3.x = fmaf(m.hi, i3x, s3.x);
+		s3.y = fmaf(m.hi, i3y, s3.y);
+	}
+	const int P = F.order;
+	const float2 ihf = F.leaf_ih_df[leaf];
+	const dfl ih = {ihf.x, ihf.y};
+	const dfc dz = {df_mul(zr.re, ih), df_mul(zr.im, ih)};
+	const double2 dl = dfc_to(horner_df(F.leaf_loc_df + ((size_t)leaf * 2 + 1) * (P + 1), P, 2, dz));
+	const float2 dzf = make_float2(dz.re.hi, dz.im.hi);
+	const float2* L3 = F.leaf_loc3f + (size_t)leaf * (P + 1);
+	float2 d2l = L3[P];
+	for (int i = P - 1; i >= 3; i--) d2l = fadd(fmulc(d2l, dzf), L3[i]);
+
+	const double2 sv = dfc_to(s2);
+	const double2 ds = smooth_dzbar_any(F, z);
+	const double a = 1 - F.kappa_tot - smooth_dz(F, z);
+	TrackEval e;
+	e.f.x = F.shear + F.theta2 * sv.x - dl.x - ds.x - a * cphi;
+	e.f.y = F.theta2 * sv.y - dl.y + ds.y + a * sphi;
+	const float2 d2s = smooth_d2zbar_f32(F, z);
+	const float t2 = (float)F.theta2;
+	e.df = make_float2(-2 * t2 * s3.x - d2l.x - d2s.x, -2 * t2 * s3.y - d2l.y + d2s.y);
+	e.pole = make_float2(2.f * pole.x, 2.f * pole.y);
+	return e;
+}
+
 /* 1/mu bound and caustic of a final point, double-float; star terms as in
    eval_f_df (leaf sums and local expansion, or ext off the root box) */
 CCF_D PointResult eval_point_df(const FieldView& F, int leaf, double2 z, double cphi, double sphi, const NearSums& ext)

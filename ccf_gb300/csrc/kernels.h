@@ -71,7 +71,9 @@ struct FieldOut
 	/* statistics */
 	unsigned long long* stats;   /* [0] max_err bits, [1] nan flag, [2] updates, [3] terms,
 	                                [4] unconverged, [5] max sweeps init, [6] max sweeps step,
-	                                [7] updates in the initial solve, [8] terms in the initial solve */
+	                                [7] updates in the initial solve, [8] terms in the initial solve,
+	                                [9] continuation rows re-run by the full-sum solver, [10] tracker
+	                                sub-step halvings, [11] TRACK_* flags of the re-run rows */
 };
 
 struct SolveArgs
@@ -89,6 +91,30 @@ struct SolveArgs
 	double2* fval;         /* [2 (row base + root) + {0, 1}]: f and f' of the sweep's active roots */
 	const float4* const* star_hilo;   /* per field, FP32 hi/lo stars (mixed) */
 	int* error;
+	const int* num_rows_dev;   /* when set, the rows to run are rows[0 .. *num_rows_dev), at most num_rows */
+};
+
+/* Per-root tracking of the continuation rows (solver.cu, track_kernel).
+   Row statistics: [3 row + 0] largest 1/mu bound (double bits), [3 row + 1]
+   TRACK_* flags, [3 row + 2] most evaluations one root needed for one phi
+   step. */
+constexpr unsigned long long TRACK_DUPLICATE = 1;    /* two roots of a column on one zero */
+constexpr unsigned long long TRACK_LOST = 2;         /* a root that did not converge */
+constexpr unsigned long long TRACK_NONFINITE = 4;    /* a non-finite 1/mu bound */
+constexpr unsigned long long TRACK_TABLE_FULL = 8;   /* the column table probe limit was reached */
+
+struct TrackArgs
+{
+	const FieldView* fields;
+	const FieldOut* outs;
+	const RowDesc* rows;        /* continuation rows; cont_base = offset of the row's column tables */
+	int num_rows;
+	const double2* master;      /* start roots (the branch centre), master[row.base + root]; read only */
+	unsigned long long* table;  /* column tables: 2 R slots per phi step, zeroed before the launch */
+	unsigned long long* row_stats;   /* 3 per row, zeroed before the launch */
+	const int* item_start;      /* [num_rows]: first work item (32 roots) of each row */
+	int num_items;
+	int* counter;               /* next work item, zeroed before the launch */
 };
 
 /* stars.cu */
@@ -126,6 +152,8 @@ void launch_leaf_df(cudaStream_t s, int num_leaves, int P, const double2* leaf_c
 /* solver.cu */
 int solver_blocks_per_sm(bool mixed);
 cudaError_t launch_solve(cudaStream_t s, const SolveArgs& a, bool mixed, bool initial);
+cudaError_t launch_track(cudaStream_t s, const TrackArgs& a, bool mixed);
+cudaError_t launch_collect_rerun(cudaStream_t s, const TrackArgs& a, RowDesc* rerun, int* count);
 cudaError_t launch_eval_points(cudaStream_t s, const FieldView* F_dev, int npts, const double2* z, const double* phi,
 	double2* f, double2* df, double2* w, double* err, double* mu);
 

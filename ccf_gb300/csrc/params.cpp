@@ -78,6 +78,11 @@ bool check_params(const ccf_params& p, bool star_input, std::string& msg)
 		return false;
 	}
 	if (p.max_iters_init < 1 || p.max_iters_step < 1) { msg = "Error. sweep caps must be >= 1."; return false; }
+	if (p.continuation != CCF_CONTINUATION_TRACK && p.continuation != CCF_CONTINUATION_ABERTH)
+	{
+		msg = "Error. continuation must be 0 (track) or 1 (aberth).";
+		return false;
+	}
 	return true;
 }
 

@@ -231,7 +231,8 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 	const int csize = (int)cluster.num_blocks();
 	const int crank = (int)cluster.block_rank();
 	const int item = blockIdx.x / csize;
-	if (item >= A.num_rows) return;
+	/* the same for every CTA of the cluster, so a cluster leaves as a whole */
+	if (item >= (A.num_rows_dev ? min(*A.num_rows_dev, A.num_rows) : A.num_rows)) return;
 
 	__shared__ FieldView sF;
 	__shared__ FieldOut sO;
@@ -668,6 +669,493 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 		atomicAdd(&st[4], s_unconv);
 		atomicMax(&st[initial ? 5 : 6], (unsigned long long)sweeps_max);
 	}
+}
+
+/* ---------------- per-root tracking of the continuation ----------------
+
+The Aberth correction of a root is the sum over the poles of f (the stars,
+double poles, and the origin for exact discs) minus the sum over the other
+roots.  Across the continuation each root starts a phi step next to the zero
+it tracks, so the far terms of both sums only rescale a step that is already
+a Newton step to ~1e-6; only the nearby poles change where a step from a
+nearby start lands.  The tracker therefore keeps the pole terms of the leaf's
+near stars (at most 32, the stars the evaluation of f visits anyway) and
+drops the O(R + N) sums: each root walks its own row with no barrier and no
+dependence on the other roots.
+
+  * predictor: the secant through the last two accepted positions in phi;
+  * corrector: z <- z - f / (f' + f S_near) until the step is below
+    1e-9 theta_star (the reference's test, include/ccf_functions.cuh:385);
+    a step that does not shrink by TRACK_CONTRACT, a non-finite step or
+    TRACK_ITERS iterations without convergence halve the phi sub-step and
+    restart from the last accepted position;
+  * check: every final root of a column is entered into that column's hash
+    table of 2^-20 theta_star cells, so two roots that converged to one zero
+    are seen (the global repulsion of the full Aberth step is what keeps the
+    reference's roots apart).  A row with such a pair, a root lost after the
+    sub-step and evaluation limits, or a non-finite 1/mu bound is run again
+    from its branch-centre roots by the full-sum continuation (solve_kernel),
+    so every row written is either a verified tracked row or the reference's
+    scheme.  Rows whose results are kept report their statistics through
+    collect_rerun_kernel; re-run rows through the full-sum kernel. */
+
+constexpr int TNT = 128;                 /* threads per CTA of the tracker */
+constexpr int TSUB = 64;                 /* one phi step in sub-step units */
+constexpr int TRACK_ITERS = 6;           /* corrector iterations before the sub-step is halved */
+constexpr double TRACK_CONTRACT = 0.5;   /* each corrector step after the first must halve */
+constexpr int TABLE_PROBES = 64;         /* linear-probe bound of the column tables (load <= 1/2) */
+constexpr double CELL_PER_THETA = 1048576.0;   /* 2^20 cells per theta_star */
+
+/* 2 sum_i 1/(z - z_i) over the near stars of the leaf; zero off the root box.
+   FP32 on the leaf-relative split positions in mixed precision (it only
+   scales the step), FP64 otherwise. */
+template <bool MIXED>
+CCF_D double2 near_pole_sum(const FieldView& F, int leaf, double2 z)
+{
+	if (leaf < 0) return make_double2(0, 0);
+	const int n = F.leaf_near_count[leaf];
+	const double2 c = F.leaf_center[leaf];
+	const double rx = z.x - c.x, ry = z.y - c.y;
+	if constexpr (MIXED)
+	{
+		const float hx = (float)rx, hy = (float)ry;
+		const float lx = (float)(rx - (double)hx), ly = (float)(ry - (double)hy);
+		const float4* P = F.leaf_near_df + (size_t)leaf * MAX_NEAR;
+		float ax = 0.f, ay = 0.f;
+		for (int i = 0; i < n; i++)
+		{
+			const float4 s = P[i];
+			const float dx = (hx - s.x) + (lx - s.z);
+			const float dy = (hy - s.y) + (ly - s.w);
+			const float r = rcp32(fmaf(dx, dx, fmaf(dy, dy, 1e-30f)));
+			ax = fmaf(dx, r, ax);
+			ay = fmaf(dy, r, ay);
+		}
+		return make_double2(2.0 * ax, -2.0 * ay);
+	}
+	else
+	{
+		const NearStar* P = F.leaf_near + (size_t)leaf * MAX_NEAR;
+		double ax = 0, ay = 0;
+		for (int i = 0; i < n; i++)
+		{
+			const NearStar s = P[i];
+			const double dx = z.x - s.x, dy = z.y - s.y;
+			const double r = rcp64(fma(dx, dx, fma(dy, dy, 1e-300)));
+			ax = fma(dx, r, ax);
+			ay = fma(dy, r, ay);
+		}
+		return make_double2(2 * ax, -2 * ay);
+	}
+}
+
+/* 64-bit key of the cell of z (never 0, the empty slot); the mixing is the
+   splitmix64 finaliser */
+CCF_D unsigned long long cell_key(double2 z, double inv_cell)
+{
+	const long long qx = __double2ll_rn(z.x * inv_cell), qy = __double2ll_rn(z.y * inv_cell);
+	unsigned long long h = (unsigned long long)qx * 0x9E3779B97F4A7C15ull ^ ((unsigned long long)qy + 0x632BE59BD9B4E019ull);
+	h ^= h >> 30;
+	h *= 0xBF58476D1CE4E5B9ull;
+	h ^= h >> 27;
+	h *= 0x94D049BB133111EBull;
+	h ^= h >> 31;
+	return h | 1ull;
+}
+
+/* enter key into an open-addressing table of `slots` entries; returns
+   TRACK_DUPLICATE when the key is already there */
+CCF_D unsigned long long table_insert(unsigned long long* tab, unsigned long long slots, unsigned long long key)
+{
+	unsigned long long s = (key >> 1) % slots;
+	for (int p = 0; p < TABLE_PROBES; p++)
+	{
+		const unsigned long long old = atomicCAS(tab + s, 0ull, key);
+		if (old == 0ull) return 0;
+		if (old == key) return TRACK_DUPLICATE;
+		s = s + 1 == slots ? 0 : s + 1;
+	}
+	return TRACK_TABLE_FULL;
+}
+
+/* secant predictor through (t0, z0) and (t1, z1) at t; constant when t0 == t1 */
+CCF_D double2 track_predict(double2 z0, int t0, double2 z1, int t1, int t)
+{
+	if (t1 == t0) return z1;
+	const double w = (double)(t - t1) / (double)(t1 - t0);
+	return make_double2(z1.x + w * (z1.x - z0.x), z1.y + w * (z1.y - z0.y));
+}
+
+/* phase at sub-step position t of a row; integer steps use row_phi */
+CCF_D double track_phi(int c, int nb, int nphi, int side, int t)
+{
+	if (t % TSUB == 0) return row_phi(c, nb, nphi, side, t / TSUB);
+	const double phi0 = PI / nb + c * 2 * PI / nb;
+	const double d = 2 * PI / nphi * ((double)t / TSUB);
+	return side == 0 ? phi0 - d : phi0 + d;
+}
+
+/* Direct star sums of the off-field points of a warp (lanes with need set) in
+   double-float on the FP32 pipe: for one such point at a time every lane
+   takes every 32nd star of the split star arrays, and the partial sums meet
+   by shuffles.  s1 when NEED1; s3 (FP32 accuracy, for f') when NEED3.  All
+   32 lanes must call it. */
+template <bool NEED1, bool NEED3>
+CCF_D void offfield_sums_warp_df(const FieldView& F, bool need, double2 z, NearSums& out)
+{
+	const unsigned full = 0xffffffffu;
+	const int lane = threadIdx.x & 31;
+	unsigned m = __ballot_sync(full, need);
+	while (m)
+	{
+		const int src = __ffs(m) - 1;
+		m &= m - 1;
+		const dfc zd = dfc_from(make_double2(__shfl_sync(full, z.x, src), __shfl_sync(full, z.y, src)));
+		SumsDF a;
+		a.s1 = {{0.f, 0.f}, {0.f, 0.f}};
+		a.s2 = a.s1;
+		dfc s3 = a.s1;
+		float2 s3f = make_float2(0.f, 0.f);
+		for (int i = lane; i < F.num_stars; i += 32)
+			star_term_df<NEED1, false>(a, s3, s3f, zd, F.star_df[i], F.star_mass_df[i]);
+		dfl w[4] = {a.s1.re, a.s1.im, a.s2.re, a.s2.im};
+#pragma unroll
+		for (int c = NEED1 ? 0 : 2; c < 4; c++)
+		{
+			for (int o = 16; o > 0; o >>= 1)
+			{
+				const dfl u = {__shfl_xor_sync(full, w[c].hi, o), __shfl_xor_sync(full, w[c].lo, o)};
+				w[c] = df_add(w[c], u);
+			}
+		}
+		if (NEED3)
+		{
+			for (int o = 16; o > 0; o >>= 1)
+			{
+				s3f.x += __shfl_xor_sync(full, s3f.x, o);
+				s3f.y += __shfl_xor_sync(full, s3f.y, o);
+			}
+		}
+		if (lane == src)
+		{
+			out.s1 = NEED1 ? make_double2(df_to_double(w[0]), df_to_double(w[1])) : make_double2(0, 0);
+			out.s2 = make_double2(df_to_double(w[2]), df_to_double(w[3]));
+			out.s3 = NEED3 ? make_double2(s3f.x, s3f.y) : make_double2(0, 0);
+		}
+	}
+}
+
+/* Is z inside the box of `leaf`?  rel = z - leaf centre. */
+CCF_D bool in_leaf_box(const FieldView& F, int leaf, double2 z, double2& rel)
+{
+	const double2 c = F.leaf_center[leaf];
+	rel = make_double2(z.x - c.x, z.y - c.y);
+	const double ih = F.leaf_inv_half[leaf];
+	return fabs(rel.x) * ih <= 1.0 && fabs(rel.y) * ih <= 1.0;
+}
+
+/* a / b in FP32 with b scaled to unit size first, so that |b|^2 neither
+   overflows nor flushes to zero (a non-finite result marks a failed step) */
+CCF_D float2 fdiv_scaled(float2 a, float2 b)
+{
+	const float m = fmaxf(fabsf(b.x), fabsf(b.y));
+	const float im = 1.f / m;
+	const float bx = b.x * im, by = b.y * im, ax = a.x * im, ay = a.y * im;
+	const float r = 1.f / (bx * bx + by * by);
+	return make_float2((ax * bx + ay * by) * r, (ay * bx - ax * by) * r);
+}
+
+CCF_D unsigned long long warp_sum_u64(unsigned long long v)
+{
+	for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+	return v;
+}
+
+/* A work item is 32 consecutive roots of one row, one warp; the rows of an
+   item come from the prefix item_start[row].  Every warp takes items from a
+   global counter until none are left, so a slow item delays only its own
+   warp and no CTA waits at a barrier for its slowest warp.  Each lane then
+   walks its root through all phi steps of the row.  Every lane of the warp
+   stays in the loops to the end: the evaluation off the root box and the
+   epilogue are warp-wide calls. */
+template <bool MIXED>
+__global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
+{
+	__shared__ FieldView sF[TNT / 32];
+	__shared__ FieldOut sO[TNT / 32];
+	__shared__ RowDesc sR[TNT / 32];
+	__shared__ double s_maxerr[TNT / 32];
+	const unsigned full = 0xffffffffu;
+	const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+	while (true)
+	{
+		int item = 0;
+		if (lane == 0) item = atomicAdd(T.counter, 1);
+		item = __shfl_sync(full, item, 0);
+		if (item >= T.num_items) break;
+		int lo = 0, hi = T.num_rows - 1;   /* the last row whose first item is <= item */
+		while (lo < hi)
+		{
+			const int mid = (lo + hi + 1) >> 1;
+			if (T.item_start[mid] <= item) lo = mid;
+			else hi = mid - 1;
+		}
+		const int row = lo;
+		__syncwarp();
+		if (lane == 0)
+		{
+			sR[w] = T.rows[row];
+			sF[w] = T.fields[sR[w].field];
+			sO[w] = T.outs[sR[w].field];
+			s_maxerr[w] = 0;
+		}
+		__syncwarp();
+		const FieldView& F = sF[w];
+		const FieldOut& O = sO[w];
+		const RowDesc& RD = sR[w];
+		const int R = F.num_roots;
+		const int a = (item - T.item_start[row]) * 32 + lane;
+		const bool valid = a < R;
+		const int c = RD.branch, side = RD.side, nb = O.nb, nphi = O.nphi;
+		const int j0 = O.step_first, j1 = O.step_last;
+		const int cap = O.max_iters_step;
+		const double tol = STEP_TOL * F.theta;
+		const double tol2 = tol * tol;
+		const bool disc_exact = !F.rectangular && !F.approx;
+		const double inv_cell = CELL_PER_THETA / F.theta;
+		const unsigned long long slots = 2ull * (unsigned long long)R;
+
+		double2 z1 = valid ? T.master[RD.base + a] : make_double2(0, 0);
+		double2 z0 = z1;
+		int t1 = (j0 - 1) * TSUB, t0 = t1;
+		bool lost = !valid;
+		int leaf = -1;
+		unsigned flags = 0;
+		unsigned long long nev = 0, nhalf = 0;
+		int maxev = 0;
+
+		for (int j = j0; j <= j1; j++)
+		{
+			const int tend = j * TSUB;
+			double sj = 0, cj = 0;
+			if (lane == 0) sincos(row_phi(c, nb, nphi, side, j), &sj, &cj);
+			sj = __shfl_sync(full, sj, 0);
+			cj = __shfl_sync(full, cj, 0);
+
+			int tt = tend;
+			double cp = cj, sp = sj;
+			double2 z = track_predict(z0, t0, z1, t1, tt);
+			bool busy = !lost;
+			int it = 0, evs = 0;
+			double prev2 = 0;
+			while (__any_sync(full, busy))
+			{
+				/* the leaf of z: the cached one while z stays in its box */
+				double2 rel = make_double2(0, 0);
+				if (busy && !(leaf >= 0 && in_leaf_box(F, leaf, z, rel)))
+				{
+					leaf = find_leaf(F, z);
+					if (leaf >= 0) in_leaf_box(F, leaf, z, rel);
+				}
+				const bool off = busy && leaf < 0;
+				double2 step;
+				double as2;
+				if constexpr (MIXED)
+				{
+					TrackEval e;
+					e.f = make_double2(0, 0);
+					e.df = make_float2(0.f, 0.f);
+					e.pole = make_float2(0.f, 0.f);
+					if (busy && leaf >= 0) e = eval_track_df(F, leaf, z, rel, cp, sp);
+					if (__any_sync(full, off))
+					{
+						/* off the root box: direct sums over every star, double-float */
+						NearSums ns = zero_sums();
+						offfield_sums_warp_df<false, true>(F, off, z, ns);
+						if (off)
+						{
+							e.f = eval_f_df(F, -1, z, cp, sp, ns);
+							e.df = eval_df32(F, -1, z, ns.s3);
+						}
+					}
+					if (!busy) continue;
+					if (disc_exact)
+					{
+						const float2 iz = finv(make_float2((float)z.x, (float)z.y));
+						e.pole.x += 2.f * iz.x;
+						e.pole.y += 2.f * iz.y;
+					}
+					const float2 f32 = make_float2((float)e.f.x, (float)e.f.y);
+					const float2 st = fdiv_scaled(f32, fadd(e.df, fmulc(f32, e.pole)));
+					step = make_double2((double)st.x, (double)st.y);
+					as2 = (double)(st.x * st.x + st.y * st.y);
+				}
+				else
+				{
+					const FdF e = eval_fdf_warp<false>(F, busy, z, leaf, false, zero_sums(), cp, sp);
+					if (!busy) continue;
+					double2 S = near_pole_sum<false>(F, leaf, z);
+					if (disc_exact)
+					{
+						const double2 iz = cinv(z);
+						S.x += 2 * iz.x;
+						S.y += 2 * iz.y;
+					}
+					step = cdiv(e.f, cadd(e.df, cmul(e.f, S)));
+					as2 = step.x * step.x + step.y * step.y;
+				}
+				evs++;
+				bool conv = false, fail = !isfinite(as2);
+				if (!fail && it > 0 && as2 >= tol2 && as2 > TRACK_CONTRACT * TRACK_CONTRACT * prev2) fail = true;
+				if (!fail)
+				{
+					z = csub(z, step);
+					it++;
+					prev2 = as2;
+					if (as2 < tol2) conv = true;
+					else if (it >= TRACK_ITERS) fail = true;
+				}
+				int tn = tt;
+				if (conv)
+				{
+					const int dist = tt - t1;
+					z0 = z1;
+					t0 = t1;
+					z1 = z;
+					t1 = tt;
+					if (tt == tend) busy = false;
+					else tn = min(t1 + 2 * dist, tend);
+				}
+				else if (fail)
+				{
+					if (tt - t1 > 1)
+					{
+						tn = t1 + (tt - t1) / 2;
+						nhalf++;
+					}
+					else
+					{
+						lost = true;
+						busy = false;
+					}
+				}
+				if (busy && evs >= cap)
+				{
+					lost = true;
+					busy = false;
+				}
+				if (busy && (conv || fail))
+				{
+					/* next target: predict, restart the corrector */
+					tt = tn;
+					z = track_predict(z0, t0, z1, t1, tt);
+					it = 0;
+					prev2 = 0;
+					if (tt == tend)
+					{
+						cp = cj;
+						sp = sj;
+					}
+					else
+					{
+						sincos(track_phi(c, nb, nphi, side, tt), &sp, &cp);
+					}
+				}
+			}
+			nev += evs;
+			maxev = max(maxev, evs);
+
+			/* outputs of step j, then the column check */
+			const bool v = !lost;
+			const int k = side == 0 ? O.half - j : O.half + j;
+			int leafo = 0;
+			if (v)
+			{
+				double2 rel;
+				leafo = (leaf >= 0 && in_leaf_box(F, leaf, z1, rel)) ? leaf : find_leaf(F, z1);
+			}
+			const size_t out = ((size_t)(v ? a : 0) * nb + c) * O.cols + k;
+			/* off-field points in double-float, as in the iterations (the
+			   length scales keep the FP64 evaluation) */
+			NearSums off = zero_sums();
+			const bool df_off = MIXED && O.mu == nullptr;
+			if (df_off) offfield_sums_warp_df<true, false>(F, v && leafo < 0, z1, off);
+			if (!point_epilogue_warp<MIXED>(F, O, v, z1, leafo, df_off && leafo < 0, off, out, cj, sj, &s_maxerr[w]))
+				flags |= (unsigned)TRACK_NONFINITE;
+			if (v)
+			{
+				unsigned long long* tab = T.table + RD.cont_base + (size_t)(j - j0) * slots;
+				flags |= (unsigned)table_insert(tab, slots, cell_key(z1, inv_cell));
+			}
+		}
+		if (valid && lost) flags |= (unsigned)TRACK_LOST;
+		flags = __reduce_or_sync(full, flags);
+		maxev = (int)__reduce_max_sync(full, (unsigned)maxev);
+		nev = warp_sum_u64(nev);
+		nhalf = warp_sum_u64(nhalf);
+		__syncwarp();
+		if (lane == 0)
+		{
+			unsigned long long* rs = T.row_stats + 3 * (size_t)row;
+			atomicMax(&rs[0], (unsigned long long)__double_as_longlong(s_maxerr[w]));
+			if (flags) atomicOr(&rs[1], (unsigned long long)flags);
+			atomicMax(&rs[2], (unsigned long long)maxev);
+			atomicAdd(&O.stats[2], nev);
+			if (nhalf) atomicAdd(&O.stats[10], nhalf);
+		}
+	}
+}
+
+/* Rows the tracker flagged go to the re-run list (and count in stats[9]);
+   the others report their largest 1/mu bound and evaluations per step. */
+__global__ void collect_rerun_kernel(const TrackArgs T, RowDesc* rerun, int* count)
+{
+	const int r = blockIdx.x * blockDim.x + threadIdx.x;
+	if (r >= T.num_rows) return;
+	const RowDesc row = T.rows[r];
+	const unsigned long long* rs = T.row_stats + 3 * (size_t)r;
+	unsigned long long* st = T.outs[row.field].stats;
+	if (rs[1])
+	{
+		const int q = atomicAdd(count, 1);
+		rerun[q] = row;
+		atomicAdd(&st[9], 1ull);
+		atomicOr(&st[11], rs[1]);
+	}
+	else
+	{
+		atomicMax(&st[0], rs[0]);
+		atomicMax(&st[6], rs[2]);
+	}
+}
+
+cudaError_t launch_track(cudaStream_t s, const TrackArgs& a, bool mixed)
+{
+	if (a.num_items == 0) return cudaSuccess;
+	/* persistent warps: as many CTAs as are resident at once */
+	static int per_sm[2] = {0, 0};
+	int& n = per_sm[mixed ? 1 : 0];
+	if (n == 0)
+	{
+		if (mixed) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, track_kernel<true>, TNT, 0);
+		else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, track_kernel<false>, TNT, 0);
+		if (n < 1) n = 1;
+	}
+	int dev = 0, sms = 0;
+	cudaGetDevice(&dev);
+	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+	const int blocks = std::max(1, std::min(sms * n, (a.num_items + TNT / 32 - 1) / (TNT / 32)));
+	if (mixed) track_kernel<true><<<blocks, TNT, 0, s>>>(a);
+	else track_kernel<false><<<blocks, TNT, 0, s>>>(a);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_collect_rerun(cudaStream_t s, const TrackArgs& a, RowDesc* rerun, int* count)
+{
+	if (a.num_rows == 0) return cudaSuccess;
+	collect_rerun_kernel<<<(a.num_rows + 127) / 128, 128, 0, s>>>(a, rerun, count);
+	return cudaGetLastError();
 }
 
 int solver_blocks_per_sm(bool mixed)

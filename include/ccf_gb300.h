@@ -53,6 +53,20 @@ typedef enum ccf_precision
 	                            circle and FP64 outside; length scales in FP64 */
 } ccf_precision;
 
+/* How the roots are carried from one phi step to the next. */
+typedef enum ccf_continuation
+{
+	CCF_CONTINUATION_TRACK = 0,  /* default: every root follows its own path in
+	                                phi with a secant predictor and a corrector
+	                                whose Aberth correction keeps the poles of the
+	                                leaf's near stars only; every column is checked
+	                                for two roots on one zero, and a row that fails
+	                                the check (or loses a root) is run again by the
+	                                full-sum continuation */
+	CCF_CONTINUATION_ABERTH = 1  /* the full Aberth step of the reference for every
+	                                root of a row (include/ccf_functions.cuh:261-394) */
+} ccf_continuation;
+
 /* Parameters.  The first block mirrors the public fields of CCF<T> with the
    same names, meanings and defaults (include/ccf.cuh:42-62); the second block
    is specific to this implementation.  Fill with ccf_default_params(). */
@@ -88,7 +102,8 @@ typedef struct ccf_params
 	int exact_binomials;         /* 1: exact binomials in the FMM translations;
 	                                0 (default): the reference's int32 table */
 	int device;                  /* CUDA device ordinal, default 0 */
-	int reserved[8];
+	int continuation;            /* ccf_continuation, default CCF_CONTINUATION_TRACK */
+	int reserved[7];
 } ccf_params;
 
 /* Derived parameters, statistics and timings of a run.  Names follow the keys
@@ -139,7 +154,12 @@ typedef struct ccf_info
 	long long kernel_launches;   /* CUDA kernels this field's run launched */
 	long long root_updates_init; /* the part of root_updates done at the branch centres */
 	long long sum_terms_init;    /* the part of sum_terms done at the branch centres */
-	double reserved[5];
+	long long rows_rerun;        /* continuation rows the tracker handed to the full-sum solver */
+	long long step_halvings;     /* phi sub-step halvings of the tracker */
+	long long rerun_flags;       /* why rows were re-run: 1 two roots on one zero, 2 a
+	                                root lost, 4 a non-finite 1/mu bound, 8 a full
+	                                column table (bits OR-ed over the rows) */
+	double reserved[2];
 } ccf_info;
 
 typedef struct ccf_handle ccf_handle;

@@ -50,9 +50,11 @@ public:
 	int write_mu_length_scales = 0;
 	std::string outfile_prefix = "./";
 
-	/* additions: solver precision (CCF_PRECISION_MIXED or CCF_PRECISION_FP64) and device */
+	/* additions: solver precision (CCF_PRECISION_MIXED or CCF_PRECISION_FP64),
+	   device and continuation (CCF_CONTINUATION_TRACK or CCF_CONTINUATION_ABERTH) */
 	int precision = CCF_PRECISION_MIXED;
 	int device = 0;
+	int continuation = CCF_CONTINUATION_TRACK;
 
 	CCF()
 	{
@@ -127,6 +129,7 @@ private:
 		p.precision = precision;
 		p.output_float = std::is_same_v<T, float> ? 1 : 0;
 		p.device = device;
+		p.continuation = continuation;
 		return ccf_set_params(h_, &p) == CCF_OK;
 	}
 };

@@ -131,3 +131,23 @@ def test_run_without_a_gpu_reports_no_device():
     c = CCF(num_stars=10, num_phi=4)
     assert not c.run(-1)
     assert c.last_status == 3 and "No CUDA capable devices" in c.last_error()
+
+
+def test_continuation_parameter():
+    """Default: per-root tracking; 1 selects the full Aberth continuation;
+    anything else is refused on the host."""
+    L = _lib.load()
+    p = _lib.CcfParams()
+    L.ccf_default_params(ctypes.byref(p))
+    assert p.continuation == _lib.CONTINUATION_TRACK
+    info = _lib.CcfInfo()
+    msg = ctypes.create_string_buffer(512)
+    for v, ok in ((0, True), (1, True), (2, False), (-1, False)):
+        p.continuation = v
+        rc = L.ccf_derive_params(ctypes.byref(p), ctypes.byref(info), msg, 512)
+        assert (rc == 0) == ok, (v, msg.value)
+        if not ok:
+            assert b"continuation must be 0 (track) or 1 (aberth)" in msg.value
+    assert derive_params(continuation="aberth")["rc"] == 0
+    with pytest.raises(ValueError):
+        derive_params(continuation="newton")

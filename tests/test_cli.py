@@ -31,6 +31,10 @@ def test_help_and_argument_errors():
     assert rc == 255 and "smooth_fraction must be >= 0" in err
     rc, _, err = run("-pr", "fp16")
     assert rc == 255 and "Invalid precision input" in err
+    rc, _, err = run("-ct", "newton")
+    assert rc == 255 and "Invalid continuation input" in err
+    rc, out, _ = run("-h")
+    assert "--continuation" in out
 
 
 @pytest.mark.gpu

@@ -7,7 +7,8 @@ allocator.  Its row scratch lives in a fixed device array inside the
 library instead.  This test gives it the branch-centre roots of a normal
 ccf_run, lets it continue both sides of a branch, two calls in a row, and
 checks every step it writes against the columns ccf_run produced for the same
-branch and side (same solver, so the tolerance of the parity tests, 1e-9
+branch and side with the full-sum continuation, which is the scheme the entry
+point runs (same solver, so the tolerance of the parity tests, 1e-9
 theta_star, is met with room to spare).  Device buffers come from torch,
 which is only plumbing here; the entry point is called through the C ABI.
 
@@ -34,6 +35,7 @@ def test_noalloc_continuation_matches_ccf_run():
         pytest.skip("needs a GPU")
     c = CCF(**CFG)
     c.write_mu_length_scales = 0
+    c.continuation = "aberth"
     assert c.run(-1), c.last_error()
     ref = c.results(stars=False)
     info = ref["info"]
