@@ -654,7 +654,7 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		CCF_TRY(P.track_table.ensure(table_slots), "cudaMalloc(tables)");
 		CCF_TRY(P.row_stats.ensure(3 * rc.size()), "cudaMalloc(rows)");
 		CCF_TRY(P.rows_rerun.ensure(rc.size()), "cudaMalloc(rows)");
-		CCF_TRY(P.rerun_count.ensure(2), "cudaMalloc(rows)");
+		CCF_TRY(P.rerun_count.ensure(3), "cudaMalloc(rows)");
 		CCF_TRY(P.item_start.ensure(rc.size()), "cudaMalloc(rows)");
 	}
 
@@ -717,9 +717,16 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		}
 		CCF_TRY(cudaMemcpyAsync(P.item_start.ptr, item_start_host.data(), rc.size() * sizeof(int), cudaMemcpyHostToDevice, s),
 			"upload");
+		CCF_TRY(P.solo.ensure((size_t)ncont + 1), "cudaMalloc(rows)");
+		CCF_TRY(P.is_solo.ensure((size_t)ncont), "cudaMalloc(rows)");
+		T.solo = P.solo.ptr;
+		T.num_solo = reinterpret_cast<int*>(P.solo.ptr + ncont);
+		T.is_solo = P.is_solo.ptr;
+		CCF_TRY(cudaMemsetAsync(T.num_solo, 0, sizeof(int), s), "memset");
 		CCF_TRY(cudaMemsetAsync(P.track_table.ptr, 0, table_slots * sizeof(unsigned long long), s), "memset");
 		CCF_TRY(cudaMemsetAsync(P.row_stats.ptr, 0, 3 * rc.size() * sizeof(unsigned long long), s), "memset");
-		CCF_TRY(cudaMemsetAsync(P.rerun_count.ptr, 0, 2 * sizeof(int), s), "memset");
+		CCF_TRY(cudaMemsetAsync(P.rerun_count.ptr, 0, 3 * sizeof(int), s), "memset");
+		CCF_TRY(launch_track_mark(s, T), "track_mark");
 		CCF_TRY(launch_track(s, T, mixed), "track_ccs");
 		CCF_TRY(launch_collect_rerun(s, T, P.rows_rerun.ptr, P.rerun_count.ptr), "collect_rerun");
 		A.rows = P.rows_rerun.ptr;
@@ -755,9 +762,10 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		info.t_ccs = ev_ms(f->ev[4], f->ev[5]) * 1e-3;
 		info.t_caustics = 0;
 		info.t_total = ev_ms(f->ev[0], f->ev[5]) * 1e-3;
-		/* root seeds, initial solve, continuation (tracker: tracking, row
-		   collection and the full-sum launch for the rows to re-run) */
-		info.kernel_launches += track ? 5 : 3;
+		/* root seeds, initial solve, continuation (tracker: item marking,
+		   tracking, row collection and the full-sum launch for the rows to
+		   re-run) */
+		info.kernel_launches += track ? 6 : 3;
 		if (info.has_nan)
 		{
 			f->error = "Error. Errors in 1/mu contain values which are not positive real numbers.";

@@ -188,20 +188,48 @@ CCF_D double2 eval_f_df(const FieldView& F, int leaf, double2 z, double cphi, do
 	return f;
 }
 
+/* Double-float constants of a field for the continuation tracker: shear,
+   theta^2, the constant 1 - kappa_tot - d alpha_smooth / dz of the
+   approximate smooth-mass forms, the constant term of d alpha_smooth / d zbar
+   of the rectangular Taylor form, and FP32 copies of 1 / corner,
+   1 / corner^2 and the squared radius inside which the Taylor form is
+   evaluated in double-float. */
+struct TrackConst
+{
+	dfl shear, theta2, a, k1;
+	float2 ic, ic2;
+	float r2;
+};
+
+CCF_D TrackConst track_const(const FieldView& F)
+{
+	TrackConst k;
+	k.shear = df_from_double(F.shear);
+	k.theta2 = df_from_double(F.theta2);
+	k.a = df_from_double(1 - F.kappa_tot - smooth_dz(F, make_double2(0, 0)));
+	k.k1 = df_from_double(F.smooth_k1);
+	k.ic = make_float2((float)F.inv_corner.x, (float)F.inv_corner.y);
+	k.ic2 = make_float2((float)F.inv_corner2.x, (float)F.inv_corner2.y);
+	k.r2 = (float)(SMOOTH_DF_RANGE * F.corner_abs * F.corner_abs);
+	return k;
+}
+
 /* What one corrector iteration of the continuation tracker needs at a root
-   inside the root box: f (double-float, as eval_f_df), f' (FP32, as
-   eval_df32) and the pole sum 2 sum_i 1/(z - z_i) over the leaf's near stars
-   (FP32), from one pass over those stars: the FP32 terms are the high words
-   of the double-float 1/d and 1/d^2 the pass forms for f.  rel = z - leaf
-   centre in FP64. */
+   inside the root box: f rounded to FP32 after its assembly in double-float
+   (only the step is taken from it), f' (FP32, as eval_df32) and the pole sum
+   2 sum_i 1/(z - z_i) over the leaf's near stars (FP32), from one pass over
+   those stars: the FP32 terms are the high words of the double-float 1/d and
+   1/d^2 the pass forms for f.  The terms of f are the ones of eval_f_df,
+   summed in double-float instead of FP64, so the FP64 pipe only splits the
+   coordinates.  rel = z - leaf centre in FP64; cph, sph = cos, sin phi. */
 struct TrackEval
 {
-	double2 f;
+	float2 f;
 	float2 df;
 	float2 pole;
 };
 
-CCF_D TrackEval eval_track_df(const FieldView& F, int leaf, double2 z, double2 rel, double cphi, double sphi)
+CCF_D TrackEval eval_track_df(const FieldView& F, const TrackConst& K, int leaf, double2 z, double2 rel, dfl cph, dfl sph)
 {
 	const dfc zr = dfc_from(rel);
 	dfc s2 = {{0.f, 0.f}, {0.f, 0.f}};
@@ -235,20 +263,52 @@ CCF_D TrackEval eval_track_df(const FieldView& F, int leaf, double2 z, double2 r
 	const float2 ihf = F.leaf_ih_df[leaf];
 	const dfl ih = {ihf.x, ihf.y};
 	const dfc dz = {df_mul(zr.re, ih), df_mul(zr.im, ih)};
-	const double2 dl = dfc_to(horner_df(F.leaf_loc_df + ((size_t)leaf * 2 + 1) * (P + 1), P, 2, dz));
+	const dfc dl = horner_df(F.leaf_loc_df + ((size_t)leaf * 2 + 1) * (P + 1), P, 2, dz);
 	const float2 dzf = make_float2(dz.re.hi, dz.im.hi);
 	const float2* L3 = F.leaf_loc3f + (size_t)leaf * (P + 1);
 	float2 d2l = L3[P];
 	for (int i = P - 1; i >= 3; i--) d2l = fadd(fmulc(d2l, dzf), L3[i]);
 
-	const double2 sv = dfc_to(s2);
-	const double2 ds = smooth_dzbar_any(F, z);
-	const double a = 1 - F.kappa_tot - smooth_dz(F, z);
+	/* smooth mass: d alpha / d zbar (double-float) and d2 alpha / d zbar2 (FP32) */
+	dfc ds;
+	float2 d2s;
+	const float zx = (float)z.x, zy = (float)z.y;
+	if (F.rectangular && F.approx && F.smooth_m > 0 && zx * zx + zy * zy < K.r2)
+	{
+		const dfc zb = dfc_from(make_double2(z.x, -z.y));
+		const dfc rr = dfc_mul(zb, dfc_load(F.inv_corner_df));
+		const dfc u = dfc_mul(rr, rr);
+		dfc acc = dfc_load(F.smooth_d1_df[F.smooth_m - 1]);
+		for (int m = F.smooth_m - 2; m >= 0; m--) acc = dfc_add(dfc_mul(acc, u), dfc_load(F.smooth_d1_df[m]));
+		ds = dfc_mul(acc, u);
+		ds.re = df_add(ds.re, K.k1);
+		const float2 zbf = make_float2(zx, -zy);
+		const float2 r = fmulc(zbf, K.ic);
+		const float2 uf = fmulc(r, r);
+		float2 a2 = F.smooth_d2f[F.smooth_m - 1];
+		for (int m = F.smooth_m - 2; m >= 0; m--) a2 = fadd(fmulc(a2, uf), F.smooth_d2f[m]);
+		d2s = fmulc(a2, fmulc(zbf, K.ic2));
+	}
+	else
+	{
+		ds = dfc_from(smooth_dzbar(F, z));
+		const double2 t = smooth_d2zbar(F, z);
+		d2s = make_float2((float)t.x, (float)t.y);
+	}
+	const dfl a = F.approx ? K.a : df_from_double(1 - F.kappa_tot - smooth_dz(F, z));
+
+	/* f = shear + theta^2 s2 - dl - conj-parts of ds - a e^{-i phi} (eval_f_df) */
+	dfl fr = df_add(K.shear, df_mul(K.theta2, s2.re));
+	fr = df_add(fr, df_neg(dl.re));
+	fr = df_add(fr, df_neg(ds.re));
+	fr = df_add(fr, df_neg(df_mul(a, cph)));
+	dfl fi = df_mul(K.theta2, s2.im);
+	fi = df_add(fi, df_neg(dl.im));
+	fi = df_add(fi, ds.im);
+	fi = df_add(fi, df_mul(a, sph));
 	TrackEval e;
-	e.f.x = F.shear + F.theta2 * sv.x - dl.x - ds.x - a * cphi;
-	e.f.y = F.theta2 * sv.y - dl.y + ds.y + a * sphi;
-	const float2 d2s = smooth_d2zbar_f32(F, z);
-	const float t2 = (float)F.theta2;
+	e.f = make_float2(fr.hi + fr.lo, fi.hi + fi.lo);
+	const float t2 = K.theta2.hi;
 	e.df = make_float2(-2 * t2 * s3.x - d2l.x - d2s.x, -2 * t2 * s3.y - d2l.y + d2s.y);
 	e.pole = make_float2(2.f * pole.x, 2.f * pole.y);
 	return e;

@@ -114,7 +114,10 @@ struct TrackArgs
 	unsigned long long* row_stats;   /* 3 per row, zeroed before the launch */
 	const int* item_start;      /* [num_rows]: first work item (32 roots) of each row */
 	int num_items;
-	int* counter;               /* next work item, zeroed before the launch */
+	int* counter;               /* [0] next solo root, [1] next item in order; zeroed before the launch */
+	int2* solo;                 /* (row, root) of the roots that start off the root box: one warp each, first ... */
+	int* num_solo;              /* ... their number (zeroed before the marking launch) */
+	unsigned char* is_solo;     /* [master index]: the root runs solo, not in its item */
 };
 
 /* stars.cu */
@@ -152,6 +155,7 @@ void launch_leaf_df(cudaStream_t s, int num_leaves, int P, const double2* leaf_c
 /* solver.cu */
 int solver_blocks_per_sm(bool mixed);
 cudaError_t launch_solve(cudaStream_t s, const SolveArgs& a, bool mixed, bool initial);
+cudaError_t launch_track_mark(cudaStream_t s, const TrackArgs& a);
 cudaError_t launch_track(cudaStream_t s, const TrackArgs& a, bool mixed);
 cudaError_t launch_collect_rerun(cudaStream_t s, const TrackArgs& a, RowDesc* rerun, int* count);
 cudaError_t launch_eval_points(cudaStream_t s, const FieldView* F_dev, int npts, const double2* z, const double* phi,

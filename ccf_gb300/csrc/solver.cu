@@ -845,6 +845,28 @@ CCF_D void offfield_sums_warp_df(const FieldView& F, bool need, double2 z, NearS
 	}
 }
 
+/* f (rounded to FP32) and f' of the warp's lanes with off set, which lie
+   outside the root box: direct double-float sums over every star.  Kept out
+   of line, as the rare path of the tracker's iteration.  All 32 lanes must
+   call it. */
+struct FdF32
+{
+	float2 f, df;
+};
+__device__ __noinline__ FdF32 track_offfield(const FieldView& F, bool off, double2 z, double cphi, double sphi)
+{
+	NearSums ns = zero_sums();
+	offfield_sums_warp_df<false, true>(F, off, z, ns);
+	FdF32 r;
+	r.f = make_float2(0.f, 0.f);
+	r.df = r.f;
+	if (!off) return r;
+	const double2 f = eval_f_df(F, -1, z, cphi, sphi, ns);
+	r.f = make_float2((float)f.x, (float)f.y);
+	r.df = eval_df32(F, -1, z, ns.s3);
+	return r;
+}
+
 /* Is z inside the box of `leaf`?  rel = z - leaf centre. */
 CCF_D bool in_leaf_box(const FieldView& F, int leaf, double2 z, double2& rel)
 {
@@ -871,6 +893,47 @@ CCF_D unsigned long long warp_sum_u64(unsigned long long v)
 	return v;
 }
 
+/* the row of a work item: the last row whose first item is <= item */
+CCF_D int item_row(const TrackArgs& T, int item)
+{
+	int lo = 0, hi = T.num_rows - 1;
+	while (lo < hi)
+	{
+		const int mid = (lo + hi + 1) >> 1;
+		if (T.item_start[mid] <= item) lo = mid;
+		else hi = mid - 1;
+	}
+	return lo;
+}
+
+/* Roots that start outside the root box evaluate f by direct sums over
+   every star, which the warp computes together, one such point at a time.  In
+   a warp of 32 tracked roots a few of them would multiply the cost of every
+   iteration of the other 31 and make their item the longest of the launch,
+   so each of these roots is tracked alone by a warp of its own (its lane 0;
+   the other lanes only help with the sums) and is left out of its item.
+   This kernel lists them (in no particular order: a root's results do not
+   depend on when or where it runs). */
+__global__ void track_mark_kernel(const TrackArgs T)
+{
+	const int item = blockIdx.x * blockDim.x + threadIdx.x;
+	if (item >= T.num_items) return;
+	const int row = item_row(T, item);
+	const RowDesc rd = T.rows[row];
+	const FieldView* F = T.fields + rd.field;
+	const int R = F->num_roots;
+	const double2 c = F->node_center[0];
+	const double h = F->node_half[0];
+	const int a0 = (item - T.item_start[row]) * 32;
+	for (int a = a0; a < min(a0 + 32, R); a++)
+	{
+		const double2 z = T.master[rd.base + a];
+		const bool off = fabs(z.x - c.x) > h || fabs(z.y - c.y) > h;
+		T.is_solo[rd.base + a] = off ? 1 : 0;
+		if (off) T.solo[atomicAdd(T.num_solo, 1)] = make_int2(row, a);
+	}
+}
+
 /* A work item is 32 consecutive roots of one row, one warp; the rows of an
    item come from the prefix item_start[row].  Every warp takes items from a
    global counter until none are left, so a slow item delays only its own
@@ -884,39 +947,54 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 	__shared__ FieldView sF[TNT / 32];
 	__shared__ FieldOut sO[TNT / 32];
 	__shared__ RowDesc sR[TNT / 32];
+	__shared__ TrackConst sK[TNT / 32];
 	__shared__ double s_maxerr[TNT / 32];
 	const unsigned full = 0xffffffffu;
 	const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
 	while (true)
 	{
-		int item = 0;
-		if (lane == 0) item = atomicAdd(T.counter, 1);
-		item = __shfl_sync(full, item, 0);
-		if (item >= T.num_items) break;
-		int lo = 0, hi = T.num_rows - 1;   /* the last row whose first item is <= item */
-		while (lo < hi)
+		/* the solo roots first, then the items in order */
+		int item = 0, solo_root = -1, row = 0;
+		if (lane == 0)
 		{
-			const int mid = (lo + hi + 1) >> 1;
-			if (T.item_start[mid] <= item) lo = mid;
-			else hi = mid - 1;
+			const int q = atomicAdd(&T.counter[0], 1);
+			if (q < *T.num_solo)
+			{
+				const int2 sr = T.solo[q];
+				row = sr.x;
+				solo_root = sr.y;
+			}
+			else
+			{
+				item = atomicAdd(&T.counter[1], 1);
+			}
 		}
-		const int row = lo;
+		item = __shfl_sync(full, item, 0);
+		solo_root = __shfl_sync(full, solo_root, 0);
+		if (solo_root < 0)
+		{
+			if (item >= T.num_items) break;
+			row = item_row(T, item);
+		}
+		row = __shfl_sync(full, row, 0);
 		__syncwarp();
 		if (lane == 0)
 		{
 			sR[w] = T.rows[row];
 			sF[w] = T.fields[sR[w].field];
 			sO[w] = T.outs[sR[w].field];
+			sK[w] = track_const(sF[w]);
 			s_maxerr[w] = 0;
 		}
 		__syncwarp();
 		const FieldView& F = sF[w];
+		const TrackConst& K = sK[w];
 		const FieldOut& O = sO[w];
 		const RowDesc& RD = sR[w];
 		const int R = F.num_roots;
-		const int a = (item - T.item_start[row]) * 32 + lane;
-		const bool valid = a < R;
+		const int a = solo_root >= 0 ? solo_root : (item - T.item_start[row]) * 32 + lane;
+		const bool valid = solo_root >= 0 ? lane == 0 : (a < R && !T.is_solo[RD.base + a]);
 		const int c = RD.branch, side = RD.side, nb = O.nb, nphi = O.nphi;
 		const int j0 = O.step_first, j1 = O.step_last;
 		const int cap = O.max_iters_step;
@@ -945,6 +1023,8 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 
 			int tt = tend;
 			double cp = cj, sp = sj;
+			const dfl cjd = df_from_double(cj), sjd = df_from_double(sj);
+			dfl cpd = cjd, spd = sjd;
 			double2 z = track_predict(z0, t0, z1, t1, tt);
 			bool busy = !lost;
 			int it = 0, evs = 0;
@@ -964,20 +1044,14 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 				if constexpr (MIXED)
 				{
 					TrackEval e;
-					e.f = make_double2(0, 0);
+					e.f = make_float2(0.f, 0.f);
 					e.df = make_float2(0.f, 0.f);
 					e.pole = make_float2(0.f, 0.f);
-					if (busy && leaf >= 0) e = eval_track_df(F, leaf, z, rel, cp, sp);
+					if (busy && leaf >= 0) e = eval_track_df(F, K, leaf, z, rel, cpd, spd);
 					if (__any_sync(full, off))
 					{
-						/* off the root box: direct sums over every star, double-float */
-						NearSums ns = zero_sums();
-						offfield_sums_warp_df<false, true>(F, off, z, ns);
-						if (off)
-						{
-							e.f = eval_f_df(F, -1, z, cp, sp, ns);
-							e.df = eval_df32(F, -1, z, ns.s3);
-						}
+						const FdF32 o = track_offfield(F, off, z, cp, sp);
+						if (off) e.f = o.f, e.df = o.df;
 					}
 					if (!busy) continue;
 					if (disc_exact)
@@ -986,8 +1060,7 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 						e.pole.x += 2.f * iz.x;
 						e.pole.y += 2.f * iz.y;
 					}
-					const float2 f32 = make_float2((float)e.f.x, (float)e.f.y);
-					const float2 st = fdiv_scaled(f32, fadd(e.df, fmulc(f32, e.pole)));
+					const float2 st = fdiv_scaled(e.f, fadd(e.df, fmulc(e.f, e.pole)));
 					step = make_double2((double)st.x, (double)st.y);
 					as2 = (double)(st.x * st.x + st.y * st.y);
 				}
@@ -1056,10 +1129,14 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 					{
 						cp = cj;
 						sp = sj;
+						cpd = cjd;
+						spd = sjd;
 					}
 					else
 					{
 						sincos(track_phi(c, nb, nphi, side, tt), &sp, &cp);
+						cpd = df_from_double(cp);
+						spd = df_from_double(sp);
 					}
 				}
 			}
@@ -1128,6 +1205,13 @@ __global__ void collect_rerun_kernel(const TrackArgs T, RowDesc* rerun, int* cou
 		atomicMax(&st[0], rs[0]);
 		atomicMax(&st[6], rs[2]);
 	}
+}
+
+cudaError_t launch_track_mark(cudaStream_t s, const TrackArgs& a)
+{
+	if (a.num_items == 0) return cudaSuccess;
+	track_mark_kernel<<<(a.num_items + 127) / 128, 128, 0, s>>>(a);
+	return cudaGetLastError();
 }
 
 cudaError_t launch_track(cudaStream_t s, const TrackArgs& a, bool mixed)

@@ -82,7 +82,7 @@ def test_tracked_field_is_checked_and_deterministic():
     # per phi step the corrector needs a few evaluations per root
     R, nb, half = info["num_roots"], cfg["num_branches"], cfg["num_phi"] // (2 * cfg["num_branches"])
     cont = info["root_updates"] - info["root_updates_init"]
-    assert cont / (R * 2 * nb * half) < 4.0
+    assert 1.0 <= cont / (R * 2 * nb * half) < 4.0
     a = run(cfg, "aberth")
     m = O.match_sets(x["ccs"], a["ccs"], nb)
     assert m["non_bijective_cols"] == 0 and m["max_dist"] <= 1e-11
