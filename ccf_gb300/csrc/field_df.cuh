@@ -191,12 +191,12 @@ CCF_D double2 eval_f_df(const FieldView& F, int leaf, double2 z, double cphi, do
 /* Double-float constants of a field for the continuation tracker: shear,
    theta^2, the constant 1 - kappa_tot - d alpha_smooth / dz of the
    approximate smooth-mass forms, the constant term of d alpha_smooth / d zbar
-   of the rectangular Taylor form, and FP32 copies of 1 / corner,
+   of the rectangular Taylor form, kappa_star / pi, and FP32 copies of 1 / corner,
    1 / corner^2 and the squared radius inside which the Taylor form is
    evaluated in double-float. */
 struct TrackConst
 {
-	dfl shear, theta2, a, k1;
+	dfl shear, theta2, a, k1, kpi;
 	float2 ic, ic2;
 	float r2;
 };
@@ -208,31 +208,47 @@ CCF_D TrackConst track_const(const FieldView& F)
 	k.theta2 = df_from_double(F.theta2);
 	k.a = df_from_double(1 - F.kappa_tot - smooth_dz(F, make_double2(0, 0)));
 	k.k1 = df_from_double(F.smooth_k1);
+	k.kpi = df_from_double(F.kappa_star / PI);
 	k.ic = make_float2((float)F.inv_corner.x, (float)F.inv_corner.y);
 	k.ic2 = make_float2((float)F.inv_corner2.x, (float)F.inv_corner2.y);
 	k.r2 = (float)(SMOOTH_DF_RANGE * F.corner_abs * F.corner_abs);
 	return k;
 }
 
-/* What one corrector iteration of the continuation tracker needs at a root
-   inside the root box: f rounded to FP32 after its assembly in double-float
-   (only the step is taken from it), f' (FP32, as eval_df32) and the pole sum
-   2 sum_i 1/(z - z_i) over the leaf's near stars (FP32), from one pass over
-   those stars: the FP32 terms are the high words of the double-float 1/d and
-   1/d^2 the pass forms for f.  The terms of f are the ones of eval_f_df,
-   summed in double-float instead of FP64, so the FP64 pipe only splits the
-   coordinates.  rel = z - leaf centre in FP64; cph, sph = cos, sin phi. */
+/* Everything one corrector iteration of the continuation tracker needs at a
+   root inside the root box, from one pass over the leaf's near stars and one
+   pair of Horner passes over its local expansion:
+
+     f      critical-curve function (double-float assembly, as eval_f_df), and
+            its FP32 rounding for the step;
+     df     f' in FP32 (as eval_df32);
+     pole   2 sum_i 1/(z - z_i) over the near stars (FP32), the Aberth
+            correction the tracker keeps;
+     wpart  the star, local and smooth-Taylor part of the lens map w
+            (as eval_point_df): w = ((1 - kappa + gamma) x, (1 - kappa - gamma) y)
+            + wpart, plus 2 kappa_star (corner.x + x) when wmode is 1 (the
+            Taylor form was evaluated here), minus smooth_alpha(z) when wmode
+            is 0; when wmode is 2, wpart is the whole of w.
+
+   The FP32 terms are the high words of the double-float 1/d and 1/d^2 the
+   pass forms for f, so the FP64 pipe only splits the coordinates.  An
+   iteration that converges writes its outputs from these values (the lens map
+   and f are first-order corrected to the stepped root). rel = z - leaf
+   centre in FP64; cph, sph = cos, sin phi. */
 struct TrackEval
 {
 	float2 f;
 	float2 df;
 	float2 pole;
+	dfc fd;
+	dfc wpart;
+	int wmode;
 };
 
 CCF_D TrackEval eval_track_df(const FieldView& F, const TrackConst& K, int leaf, double2 z, double2 rel, dfl cph, dfl sph)
 {
 	const dfc zr = dfc_from(rel);
-	dfc s2 = {{0.f, 0.f}, {0.f, 0.f}};
+	dfc s1 = {{0.f, 0.f}, {0.f, 0.f}}, s2 = s1;
 	float2 s3 = make_float2(0.f, 0.f), pole = make_float2(0.f, 0.f);
 	const int n = F.leaf_near_count[leaf];
 	const float4* Pn = F.leaf_near_df + (size_t)leaf * MAX_NEAR;
@@ -252,6 +268,8 @@ CCF_D TrackEval eval_track_df(const FieldView& F, const TrackConst& K, int leaf,
 		i2y = {2.f * i2y.hi, 2.f * i2y.lo};                        /* 1/d^2 */
 		s2.re = df_add_fast(s2.re, df_mul(m, i2x));
 		s2.im = df_add_fast(s2.im, df_mul(m, i2y));
+		s1.re = df_add_fast(s1.re, df_mul(m, ix));
+		s1.im = df_add_fast(s1.im, df_mul(m, iy));
 		pole.x += ix.hi;
 		pole.y += iy.hi;
 		const float i3x = i2x.hi * ix.hi - i2y.hi * iy.hi;
@@ -263,25 +281,37 @@ CCF_D TrackEval eval_track_df(const FieldView& F, const TrackConst& K, int leaf,
 	const float2 ihf = F.leaf_ih_df[leaf];
 	const dfl ih = {ihf.x, ihf.y};
 	const dfc dz = {df_mul(zr.re, ih), df_mul(zr.im, ih)};
-	const dfc dl = horner_df(F.leaf_loc_df + ((size_t)leaf * 2 + 1) * (P + 1), P, 2, dz);
+	const float4* L = F.leaf_loc_df + (size_t)leaf * 2 * (P + 1);
+	const dfc al = horner_df(L, P, 1, dz);
+	const dfc dl = horner_df(L + (P + 1), P, 2, dz);
 	const float2 dzf = make_float2(dz.re.hi, dz.im.hi);
 	const float2* L3 = F.leaf_loc3f + (size_t)leaf * (P + 1);
 	float2 d2l = L3[P];
 	for (int i = P - 1; i >= 3; i--) d2l = fadd(fmulc(d2l, dzf), L3[i]);
 
-	/* smooth mass: d alpha / d zbar (double-float) and d2 alpha / d zbar2 (FP32) */
-	dfc ds;
+	/* smooth mass: d alpha / d zbar (double-float), d2 alpha / d zbar2 (FP32)
+	   and the Taylor part of alpha (double-float) */
+	TrackEval e;
+	dfc ds, sa = {{0.f, 0.f}, {0.f, 0.f}};
 	float2 d2s;
 	const float zx = (float)z.x, zy = (float)z.y;
-	if (F.rectangular && F.approx && F.smooth_m > 0 && zx * zx + zy * zy < K.r2)
+	const bool taylor = F.rectangular && F.approx && F.smooth_m > 0 && zx * zx + zy * zy < K.r2;
+	e.wmode = taylor ? 1 : 0;
+	if (taylor)
 	{
 		const dfc zb = dfc_from(make_double2(z.x, -z.y));
-		const dfc rr = dfc_mul(zb, dfc_load(F.inv_corner_df));
-		const dfc u = dfc_mul(rr, rr);
+		const dfc wc = dfc_mul(zb, dfc_load(F.inv_corner_df));   /* zbar / c */
+		const dfc u = dfc_mul(wc, wc);
 		dfc acc = dfc_load(F.smooth_d1_df[F.smooth_m - 1]);
 		for (int m = F.smooth_m - 2; m >= 0; m--) acc = dfc_add(dfc_mul(acc, u), dfc_load(F.smooth_d1_df[m]));
 		ds = dfc_mul(acc, u);
 		ds.re = df_add(ds.re, K.k1);
+		const int na = F.taylor_smooth + 1;
+		dfc aa = dfc_load(F.smooth_a_df[na]);
+		for (int i = na - 1; i >= 0; i--) aa = dfc_add(dfc_mul(aa, wc), dfc_load(F.smooth_a_df[i]));
+		/* (0, -k / pi) A: re = (k / pi) A.im, im = -(k / pi) A.re */
+		sa.re = df_mul(K.kpi, aa.im);
+		sa.im = df_neg(df_mul(K.kpi, aa.re));
 		const float2 zbf = make_float2(zx, -zy);
 		const float2 r = fmulc(zbf, K.ic);
 		const float2 uf = fmulc(r, r);
@@ -297,7 +327,7 @@ CCF_D TrackEval eval_track_df(const FieldView& F, const TrackConst& K, int leaf,
 	}
 	const dfl a = F.approx ? K.a : df_from_double(1 - F.kappa_tot - smooth_dz(F, z));
 
-	/* f = shear + theta^2 s2 - dl - conj-parts of ds - a e^{-i phi} (eval_f_df) */
+	/* f = shear + theta^2 s2 - dl - conj(ds) - a e^{-i phi} (eval_f_df) */
 	dfl fr = df_add(K.shear, df_mul(K.theta2, s2.re));
 	fr = df_add(fr, df_neg(dl.re));
 	fr = df_add(fr, df_neg(ds.re));
@@ -306,11 +336,19 @@ CCF_D TrackEval eval_track_df(const FieldView& F, const TrackConst& K, int leaf,
 	fi = df_add(fi, df_neg(dl.im));
 	fi = df_add(fi, ds.im);
 	fi = df_add(fi, df_mul(a, sph));
-	TrackEval e;
+	e.fd = {fr, fi};
 	e.f = make_float2(fr.hi + fr.lo, fi.hi + fi.lo);
 	const float t2 = K.theta2.hi;
 	e.df = make_float2(-2 * t2 * s3.x - d2l.x - d2s.x, -2 * t2 * s3.y - d2l.y + d2s.y);
 	e.pole = make_float2(2.f * pole.x, 2.f * pole.y);
+	/* w - the linear terms: (-theta^2 s1.x - al.x - sa.x, theta^2 s1.y + al.y - sa.y) (eval_point_df) */
+	dfl wr = df_neg(df_mul(K.theta2, s1.re));
+	wr = df_add(wr, df_neg(al.re));
+	wr = df_add(wr, df_neg(sa.re));
+	dfl wi = df_mul(K.theta2, s1.im);
+	wi = df_add(wi, al.im);
+	wi = df_add(wi, df_neg(sa.im));
+	e.wpart = {wr, wi};
 	return e;
 }
 

@@ -872,25 +872,28 @@ CCF_D void offfield_sums_warp_df(const FieldView& F, bool need, double2 z, NearS
 	}
 }
 
-/* f (rounded to FP32) and f' of the warp's lanes with off set, which lie
-   outside the root box: direct double-float sums over every star.  Kept out
-   of line, as the rare path of the tracker's iteration.  All 32 lanes must
-   call it. */
-struct FdF32
-{
-	float2 f, df;
-};
-__device__ __noinline__ FdF32 track_offfield(const FieldView& F, bool off, double2 z, double cphi, double sphi)
+/* The iteration quantities of the tracker (TrackEval) for the warp's lanes
+   with off set, which lie outside the root box: direct double-float sums over
+   every star, f, f' and the whole lens map (wmode 2) from the off-field
+   evaluators.  Kept out of line, as the rare path of the iteration.  All 32
+   lanes must call it. */
+__device__ __noinline__ TrackEval track_offfield(const FieldView& F, bool off, double2 z, double cphi, double sphi)
 {
 	NearSums ns = zero_sums();
-	offfield_sums_warp_df<false, true>(F, off, z, ns);
-	FdF32 r;
+	offfield_sums_warp_df<true, true>(F, off, z, ns);
+	TrackEval r;
 	r.f = make_float2(0.f, 0.f);
 	r.df = r.f;
+	r.pole = r.f;
+	r.fd = {{0.f, 0.f}, {0.f, 0.f}};
+	r.wpart = r.fd;
+	r.wmode = 2;
 	if (!off) return r;
 	const double2 f = eval_f_df(F, -1, z, cphi, sphi, ns);
+	r.fd = dfc_from(f);
 	r.f = make_float2((float)f.x, (float)f.y);
 	r.df = eval_df32(F, -1, z, ns.s3);
+	r.wpart = dfc_from(eval_point_df(F, -1, z, cphi, sphi, ns).w);
 	return r;
 }
 
@@ -961,13 +964,51 @@ __global__ void track_mark_kernel(const TrackArgs T)
 	}
 }
 
+/* phases of the whole steps of a row: cos, sin in FP64 and double-float */
+struct PhaseEntry
+{
+	double2 cs;
+	float4 cs_df;
+};
+constexpr int TRACK_TAB = 128;   /* whole steps per row held in shared memory */
+
+/* cos, sin of sub-step position t of a row: the table for whole steps, else
+   computed */
+CCF_D void track_phase(const PhaseEntry* tab, int tab_n, int c, int nb, int nphi, int side, int j0, int t, double& cp,
+	double& sp, dfl& cpd, dfl& spd)
+{
+	const int q = t / TSUB - (j0 - 1);
+	if (t % TSUB == 0 && q < tab_n)
+	{
+		const PhaseEntry e = tab[q];
+		cp = e.cs.x;
+		sp = e.cs.y;
+		cpd = {e.cs_df.x, e.cs_df.z};
+		spd = {e.cs_df.y, e.cs_df.w};
+		return;
+	}
+	sincos(track_phi(c, nb, nphi, side, t), &sp, &cp);
+	cpd = df_from_double(cp);
+	spd = df_from_double(sp);
+}
+
 /* A work item is 32 consecutive roots of one row, one warp; the rows of an
    item come from the prefix item_start[row].  Every warp takes items from a
    global counter until none are left, so a slow item delays only its own
-   warp and no CTA waits at a barrier for its slowest warp.  Each lane then
-   walks its root through all phi steps of the row.  Every lane of the warp
-   stays in the loops to the end: the evaluation off the root box and the
-   epilogue are warp-wide calls. */
+   warp and no CTA waits at a barrier for its slowest warp.
+
+   Each lane walks its own root through the phi steps of the row: one
+   evaluation per iteration of the warp's loop, whatever step and sub-step
+   the lane is at, so a lane that converges in one evaluation does not wait
+   for a neighbour that needs three.  In mixed precision an evaluation
+   carries everything the outputs need (TrackEval): a lane that converges
+   writes its root, 1/mu bound and caustic at once, first-order corrected to
+   the stepped root (the step is below 1e-9 theta_star; the lens map has
+   dw/dz = a, dw/dzbar = conj(f + a e^{-i phi}), and f is holomorphic, so
+   the remainders are O(step^2)).  The FP64 solver and the length scales use
+   the direct evaluation of the outputs (a warp-wide call).  Every lane of the
+   warp stays in the loop to the end: the evaluation off the root box and
+   the direct epilogue are warp-wide calls. */
 template <bool MIXED>
 __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 {
@@ -978,10 +1019,12 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 	__shared__ double s_maxerr[TNT / 32];
 	__shared__ double2 s_hz[TRACK_HIST * TNT];   /* accepted positions of each lane's root, newest first */
 	__shared__ int s_ht[TRACK_HIST * TNT];
+	__shared__ PhaseEntry s_tab[TNT / 32][TRACK_TAB];
 	const unsigned full = 0xffffffffu;
 	const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	double2* const hz = s_hz + threadIdx.x;
 	int* const ht = s_ht + threadIdx.x;
+	PhaseEntry* const tab = s_tab[w];
 
 	while (true)
 	{
@@ -1020,9 +1063,9 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 		}
 		__syncwarp();
 		const FieldView& F = sF[w];
-		const TrackConst& K = sK[w];
 		const FieldOut& O = sO[w];
 		const RowDesc& RD = sR[w];
+		const TrackConst& K = sK[w];
 		const int R = F.num_roots;
 		const int a = solo_root >= 0 ? solo_root : (item - T.item_start[row]) * 32 + lane;
 		const bool valid = solo_root >= 0 ? lane == 0 : (a < R && !T.is_solo[RD.base + a]);
@@ -1034,59 +1077,70 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 		const bool disc_exact = !F.rectangular && !F.approx;
 		const double inv_cell = CELL_PER_THETA / F.theta;
 		const unsigned long long slots = 2ull * (unsigned long long)R;
+		const bool direct_out = !MIXED || O.mu != nullptr;
+
+		/* phases of the row's whole steps j0 - 1 .. j1 */
+		const int tab_n = min(j1 - j0 + 2, TRACK_TAB);
+		for (int q = lane; q < tab_n; q += 32)
+		{
+			double sp, cp;
+			sincos(row_phi(c, nb, nphi, side, j0 - 1 + q), &sp, &cp);
+			const dfl cd = df_from_double(cp), sd = df_from_double(sp);
+			tab[q].cs = make_double2(cp, sp);
+			tab[q].cs_df = make_float4(cd.hi, sd.hi, cd.lo, sd.lo);
+		}
+		__syncwarp();
 
 		double2 z1 = valid ? T.master[RD.base + a] : make_double2(0, 0);
 		int t1 = (j0 - 1) * TSUB;
 		hz[0] = z1;
 		ht[0] = t1;
 		int hn = 1;
-		bool lost = !valid;
 		int leaf = -1;
 		unsigned flags = 0;
 		unsigned long long nev = 0, nhalf = 0;
 		int maxev = 0;
 
-		for (int j = j0; j <= j1; j++)
-		{
-			const int tend = j * TSUB;
-			double sj = 0, cj = 0;
-			if (lane == 0) sincos(row_phi(c, nb, nphi, side, j), &sj, &cj);
-			sj = __shfl_sync(full, sj, 0);
-			cj = __shfl_sync(full, cj, 0);
+		int j = j0;
+		bool act = valid;
+		int tt = j * TSUB;
+		double2 z = z1;
+		double cp = 0, sp = 0;
+		dfl cpd = {0.f, 0.f}, spd = {0.f, 0.f};
+		track_phase(tab, tab_n, c, nb, nphi, side, j0, tt, cp, sp, cpd, spd);
+		int it = 0, evs = 0;
+		double prev2 = 0;
+		bool lost = !valid;
 
-			int tt = tend;
-			double cp = cj, sp = sj;
-			const dfl cjd = df_from_double(cj), sjd = df_from_double(sj);
-			dfl cpd = cjd, spd = sjd;
-			double2 z = track_predict(hz, ht, hn, tt);
-			bool busy = !lost;
-			int it = 0, evs = 0;
-			double prev2 = 0;
-			while (__any_sync(full, busy))
+		while (__any_sync(full, act))
+		{
+			/* the leaf of z: the cached one while z stays in its box */
+			double2 rel = make_double2(0, 0);
+			if (act && !(leaf >= 0 && in_leaf_box(F, leaf, z, rel)))
 			{
-				/* the leaf of z: the cached one while z stays in its box */
-				double2 rel = make_double2(0, 0);
-				if (busy && !(leaf >= 0 && in_leaf_box(F, leaf, z, rel)))
+				leaf = find_leaf(F, z);
+				if (leaf >= 0) in_leaf_box(F, leaf, z, rel);
+			}
+			const bool off = act && leaf < 0;
+			double2 step = make_double2(0, 0);
+			double as2 = 0;
+			TrackEval e;
+			e.f = make_float2(0.f, 0.f);
+			e.df = e.f;
+			e.pole = e.f;
+			e.fd = {{0.f, 0.f}, {0.f, 0.f}};
+			e.wpart = e.fd;
+			e.wmode = 2;
+			if constexpr (MIXED)
+			{
+				if (act && leaf >= 0) e = eval_track_df(F, K, leaf, z, rel, cpd, spd);
+				if (__any_sync(full, off))
 				{
-					leaf = find_leaf(F, z);
-					if (leaf >= 0) in_leaf_box(F, leaf, z, rel);
+					const TrackEval o = track_offfield(F, off, z, cp, sp);
+					if (off) e = o;
 				}
-				const bool off = busy && leaf < 0;
-				double2 step;
-				double as2;
-				if constexpr (MIXED)
+				if (act)
 				{
-					TrackEval e;
-					e.f = make_float2(0.f, 0.f);
-					e.df = make_float2(0.f, 0.f);
-					e.pole = make_float2(0.f, 0.f);
-					if (busy && leaf >= 0) e = eval_track_df(F, K, leaf, z, rel, cpd, spd);
-					if (__any_sync(full, off))
-					{
-						const FdF32 o = track_offfield(F, off, z, cp, sp);
-						if (off) e.f = o.f, e.df = o.df;
-					}
-					if (!busy) continue;
 					if (disc_exact)
 					{
 						const float2 iz = finv(make_float2((float)z.x, (float)z.y));
@@ -1097,10 +1151,12 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 					step = make_double2((double)st.x, (double)st.y);
 					as2 = (double)(st.x * st.x + st.y * st.y);
 				}
-				else
+			}
+			else
+			{
+				const FdF g = eval_fdf_warp<false>(F, act, z, leaf, false, zero_sums(), cp, sp);
+				if (act)
 				{
-					const FdF e = eval_fdf_warp<false>(F, busy, z, leaf, false, zero_sums(), cp, sp);
-					if (!busy) continue;
 					double2 S = near_pole_sum<false>(F, leaf, z);
 					if (disc_exact)
 					{
@@ -1108,20 +1164,31 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 						S.x += 2 * iz.x;
 						S.y += 2 * iz.y;
 					}
-					step = cdiv(e.f, cadd(e.df, cmul(e.f, S)));
+					step = cdiv(g.f, cadd(g.df, cmul(g.f, S)));
 					as2 = step.x * step.x + step.y * step.y;
 				}
+			}
+
+			/* the lane's decision; an output step that converged is written
+			   here (mixed precision) or by the direct epilogue below */
+			bool emit = false;
+			double2 zf = make_double2(0, 0);
+			size_t out = 0;
+			double ecp = 0, esp = 0;
+			if (act)
+			{
+				nev++;
 				evs++;
 				bool conv = false, fail = !isfinite(as2);
 				if (!fail && it > 0 && as2 >= tol2 && as2 > TRACK_CONTRACT * TRACK_CONTRACT * prev2) fail = true;
 				if (!fail)
 				{
-					z = csub(z, step);
 					it++;
 					prev2 = as2;
 					if (as2 < tol2) conv = true;
 					else if (it >= TRACK_ITERS) fail = true;
 				}
+				if (!fail) z = csub(z, step);
 				int tn = tt;
 				if (conv)
 				{
@@ -1136,8 +1203,65 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 					t1 = tt;
 					hz[0] = z1;
 					ht[0] = t1;
-					if (tt == tend) busy = false;
-					else tn = min(t1 + 2 * dist, tend);
+					if (tt == j * TSUB)
+					{
+						emit = true;
+						zf = z;
+						ecp = cp;
+						esp = sp;
+						const int k = side == 0 ? O.half - j : O.half + j;
+						out = ((size_t)a * nb + c) * O.cols + k;
+						if constexpr (MIXED)
+						{
+							if (!direct_out)
+							{
+								/* the lens map at the evaluated point, then corrected to
+								   zf = ze - s: w(zf) = w(ze) - a s - (conj(f) + a e^{i phi}) conj(s) */
+								const double2 ze = make_double2(zf.x + step.x, zf.y + step.y);
+								double2 wv;
+								if (e.wmode == 2) wv = dfc_to(e.wpart);
+								else
+								{
+									const double2 wp = dfc_to(e.wpart);
+									wv.x = (1 - F.kappa_tot + F.shear) * ze.x + wp.x;
+									wv.y = (1 - F.kappa_tot - F.shear) * ze.y + wp.y;
+									if (e.wmode == 1) wv.x += 2 * F.kappa_star * (F.corner.x + ze.x);
+									else
+									{
+										const double2 sa = smooth_alpha(F, ze);
+										wv.x -= sa.x;
+										wv.y -= sa.y;
+									}
+								}
+								const double av = 1 - F.kappa_tot - smooth_dz(F, ze);
+								const double2 fz = dfc_to(e.fd);
+								const double gx = fz.x + av * cp, gy = -fz.y + av * sp;
+								wv.x -= av * step.x + gx * step.x + gy * step.y;
+								wv.y -= av * step.y - gx * step.y + gy * step.x;
+								/* f at zf: f(ze) - f' s, with a bound on the FP32 error of f' s */
+								const float2 fs = fmulc(e.df, make_float2((float)step.x, (float)step.y));
+								const double fx = fz.x - (double)fs.x, fy = fz.y - (double)fs.y;
+								const double af = hypot(fx, fy) + 1e-6 * (double)hypotf(fs.x, fs.y);
+								const double err = fmax(fabs(af * (af + 2 * av)), fabs(af * (af - 2 * av)));
+								O.ccs[out] = zf;
+								O.errs[out] = err;
+								if (O.caustics) O.caustics[out] = wv;
+								if (isfinite(err)) atomicMax((unsigned long long*)&s_maxerr[w], (unsigned long long)__double_as_longlong(err));
+								else flags |= (unsigned)TRACK_NONFINITE;
+							}
+						}
+						flags |= (unsigned)table_insert(T.table + RD.cont_base + (size_t)(j - j0) * slots, slots,
+							cell_key(zf, inv_cell));
+						maxev = max(maxev, evs);
+						evs = 0;
+						j++;
+						if (j > j1) act = false;
+						tn = j * TSUB;
+					}
+					else
+					{
+						tn = min(t1 + 2 * dist, j * TSUB);
+					}
 				}
 				else if (fail)
 				{
@@ -1149,60 +1273,37 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 					else
 					{
 						lost = true;
-						busy = false;
+						act = false;
 					}
 				}
-				if (busy && evs >= cap)
+				if (act && evs >= cap)
 				{
 					lost = true;
-					busy = false;
+					act = false;
 				}
-				if (busy && (conv || fail))
+				if (act && (conv || fail))
 				{
 					/* next target: predict, restart the corrector */
 					tt = tn;
 					z = track_predict(hz, ht, hn, tt);
 					it = 0;
 					prev2 = 0;
-					if (tt == tend)
-					{
-						cp = cj;
-						sp = sj;
-						cpd = cjd;
-						spd = sjd;
-					}
-					else
-					{
-						sincos(track_phi(c, nb, nphi, side, tt), &sp, &cp);
-						cpd = df_from_double(cp);
-						spd = df_from_double(sp);
-					}
+					track_phase(tab, tab_n, c, nb, nphi, side, j0, tt, cp, sp, cpd, spd);
 				}
 			}
-			nev += evs;
-			maxev = max(maxev, evs);
 
-			/* outputs of step j, then the column check */
-			const bool v = !lost;
-			const int k = side == 0 ? O.half - j : O.half + j;
-			int leafo = 0;
-			if (v)
+			/* direct outputs (FP64 solver, length scales): warp-wide */
+			const bool emit_direct = direct_out && emit;
+			if (__any_sync(full, emit_direct))
 			{
-				double2 rel;
-				leafo = (leaf >= 0 && in_leaf_box(F, leaf, z1, rel)) ? leaf : find_leaf(F, z1);
-			}
-			const size_t out = ((size_t)(v ? a : 0) * nb + c) * O.cols + k;
-			/* off-field points in double-float, as in the iterations (the
-			   length scales keep the FP64 evaluation) */
-			NearSums off = zero_sums();
-			const bool df_off = MIXED && O.mu == nullptr;
-			if (df_off) offfield_sums_warp_df<true, false>(F, v && leafo < 0, z1, off);
-			if (!point_epilogue_warp<MIXED>(F, O, v, z1, leafo, df_off && leafo < 0, off, out, cj, sj, &s_maxerr[w]))
-				flags |= (unsigned)TRACK_NONFINITE;
-			if (v)
-			{
-				unsigned long long* tab = T.table + RD.cont_base + (size_t)(j - j0) * slots;
-				flags |= (unsigned)table_insert(tab, slots, cell_key(z1, inv_cell));
+				int leafo = 0;
+				if (emit_direct)
+				{
+					double2 r2;
+					leafo = (leaf >= 0 && in_leaf_box(F, leaf, zf, r2)) ? leaf : find_leaf(F, zf);
+				}
+				if (!point_epilogue_warp<MIXED>(F, O, emit_direct, zf, leafo, false, zero_sums(), out, ecp, esp, &s_maxerr[w]))
+					flags |= (unsigned)TRACK_NONFINITE;
 			}
 		}
 		if (valid && lost) flags |= (unsigned)TRACK_LOST;
