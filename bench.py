@@ -205,10 +205,10 @@ class ClockSampler:
 
 # DRAM bytes (read + write) of the continuation launch per continuation point,
 # from the ncu capture summarised in
-# profiles/solve_kernel_cont_n2000_salpeter_phi512.md: 115.3 MB for the
-# 4056 * 512 points of that launch.  The traffic is the outputs plus snapshot
-# and star reads, so it grows with the points written.
-CONT_DRAM_BYTES_PER_POINT = 115.3e6 / (4056 * 512)
+# profiles/track_kernel_n2000_salpeter_phi512.md: 94.4 MB for the 4056 * 512
+# continuation points of that launch (the 40-byte outputs and the column
+# tables; leaf records and stars stay in L2).  It grows with the points written.
+CONT_DRAM_BYTES_PER_POINT = 94.4e6 / (4056 * 512)
 
 
 def hbm_peak_gbs() -> float | None:
@@ -227,6 +227,25 @@ def measure_peaks() -> dict:
         return json.loads(out)
     except Exception as e:  # noqa: BLE001
         return {"error": str(e)}
+
+
+def tracker_flops_per_eval(info: dict, approx: int) -> float:
+    """FP32 operations of one evaluation of the continuation tracker
+    (eval_track_df), counted from its double-float primitives: two_sum 6,
+    fast_two_sum 3, df_add 20, df_add_fast 11, df_mul 7, df_sqr 7, df_rcp 30;
+    a complex double-float Horner step 81.  Per near star 234 (1/d, 1/d^2, the
+    m/d and m/d^2 sums in double-float, pole and m/d^3 in FP32); the alpha and
+    d alpha/d zbar Horner passes over the local expansion; the FP32 f' pass; for
+    the rectangular Taylor smooth mass the d alpha/d zbar and alpha series;
+    about 200 for the assembly of f, the step and the bookkeeping."""
+    n = info["near_mean"]
+    P = info["expansion_order"]
+    per = 234.0 * n + 81.0 * (2 * P - 3) + 8.0 * max(P - 3, 0) + 200.0
+    if info["rectangular"] and approx:
+        ts = info["taylor_smooth"]
+        m = (ts - 1) // 2
+        per += 81.0 * (max(m - 1, 0) + ts + 1) + 8.0 * max(m - 1, 0) + 250.0
+    return per
 
 
 def algorithmic_flops(info: dict, continuation_only: bool = True, n_near: int = 32) -> float:
@@ -287,7 +306,7 @@ def run_multi(args) -> None:
 
     line = {"metric": METRIC, "unit": "points/s", "n_gpus": ws, "steps": args.steps, "warmup": max(3, args.warmup),
             "higher_is_better": True, "vs_baseline": None, "data": "synthetic (seeded star fields)",
-            "dtype": "f32+df32+f64 (FP32 correction sums, double-float f and caustics, FP64 off the corner circle)"}
+            "dtype": "f32+df32+f64 (double-float f and caustics, FP32 f' and step, FP64 coordinates)"}
     with ClockSampler(local) as clocks:
         if args.workload == "batch_256_fields_n50_1000_disc":
             fields = batch_fields()
@@ -531,7 +550,8 @@ def main() -> None:
     peaks = measure_peaks()
     t_cont = statistics.median(i["t_ccs"] for i in infos)
     cont_share = t_cont / statistics.median(i["t_total"] for i in infos)
-    flops = algorithmic_flops(info, continuation_only=True)
+    evals_cont = info["root_updates"] - info["root_updates_init"]
+    flops = evals_cont * tracker_flops_per_eval(info, cfg.get("approx", 1))
     achieved = flops / t_cont / 1e12 if t_cont > 0 else 0.0
     peak32 = peaks.get("fp32_tflops")
     traffic = CONT_DRAM_BYTES_PER_POINT * info["num_roots"] * cfg["num_phi"]
@@ -568,6 +588,25 @@ def main() -> None:
         fp64 = {"value": points / statistics.median(tt), "unit": "points/s",
                 "ms_per_step": 1e3 * statistics.median(tt)}
 
+    # the reference's continuation scheme (full Aberth step for every root of a
+    # row) on the same field and GPU, both precisions, for fields small enough
+    # to run it in seconds
+    full_sum = None
+    if args.precision == "mixed" and args.fp64_steps > 0 and cfg["num_stars"] <= 5000:
+        full_sum = {"unit": "points/s"}
+        for prec in ("mixed", "fp64"):
+            g = make(prec)
+            g.continuation = "aberth"
+            assert g.run(-1), g.last_error()
+            tt = []
+            for _ in range(args.fp64_steps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                assert g.run(-1), g.last_error()
+                tt.append(g.info()["t_total"])
+            full_sum[prec] = points / statistics.median(tt)
+            full_sum[prec + "_ms_per_step"] = 1e3 * statistics.median(tt)
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -580,7 +619,7 @@ def main() -> None:
             "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": ws, "steps": args.steps,
             "warmup": max(3, args.warmup), "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32+df32+f64 (FP32 correction sums, double-float f and caustics, FP64 off the corner circle)" if args.precision == "mixed" else "f64",
+            "dtype": "f32+df32+f64 (double-float f and caustics, FP32 f' and step, FP64 coordinates)" if args.precision == "mixed" else "f64",
             "data": "synthetic (seeded star field)",
             "config": {"workload": args.workload, **cfg, "precision": args.precision,
                        "l2": "flushed before every timed step (256 MiB write)", "parallelism": f"replicas x{ws}"},
@@ -588,15 +627,18 @@ def main() -> None:
                     "d2h_bytes_per_step": d2h},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
                          "frac": (achieved / peak32) if peak32 else None, "traffic": traffic,
-                         "kernel": "solve_kernel (phi continuation)", "kernel_share_of_step": cont_share,
+                         "kernel": "track_kernel (phi continuation)", "kernel_share_of_step": cont_share,
+                         "flops_per_evaluation": tracker_flops_per_eval(info, cfg.get("approx", 1)),
+                         "evaluations": evals_cont,
                          "peak_source": "ccf_gb300/lib/ccf_peaks (FFMA chains, measured)",
                          "fp64_peak_tflops": peaks.get("fp64_tflops"),
                          "traffic_source": "per-point DRAM bytes of the ncu capture in "
-                                           "profiles/solve_kernel_cont_n2000_salpeter_phi512.md, scaled by points",
+                                           "profiles/track_kernel_n2000_salpeter_phi512.md, scaled by points",
                          "hbm_gbs": traffic / t_cont / 1e9 if t_cont > 0 else None,
                          "hbm_peak_gbs": hbm_peak, "hbm_frac": (traffic / t_cont / 1e9 / hbm_peak)
                          if (t_cont > 0 and hbm_peak) else None},
             "fp64_plain": fp64,
+            "full_sum_continuation": full_sum,
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
             "gpu_launches": int(info["kernel_launches"]) * args.steps,
@@ -604,7 +646,9 @@ def main() -> None:
                        "expansion_order": info["expansion_order"], "max_error_1/mu": info["max_error"],
                        "unconverged": info["unconverged"], "sweeps_init": info["max_sweeps_init"],
                        "sweeps_step": info["max_sweeps_step"], "root_updates": info["root_updates"],
-                       "sum_terms": info["sum_terms"], "t_stars": info["t_stars"], "t_tree": info["t_tree"],
+                       "sum_terms": info["sum_terms"], "rows_rerun": info["rows_rerun"],
+                       "step_halvings": info["step_halvings"], "near_mean": info["near_mean"],
+                       "t_stars": info["t_stars"], "t_tree": info["t_tree"],
                        "t_init_roots": info["t_init_roots"], "t_ccs": info["t_ccs"], "peaks": peaks},
         }
         print(json.dumps(line), flush=True)

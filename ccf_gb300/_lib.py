@@ -108,7 +108,8 @@ class CcfInfo(ctypes.Structure):
         ("rows_rerun", ctypes.c_longlong),
         ("step_halvings", ctypes.c_longlong),
         ("rerun_flags", ctypes.c_longlong),
-        ("reserved", ctypes.c_double * 2),
+        ("near_mean", ctypes.c_double),
+        ("reserved", ctypes.c_double * 1),
     ]
 
     def as_dict(self) -> dict:

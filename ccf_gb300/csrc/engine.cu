@@ -405,6 +405,17 @@ ccf_status Engine::build_fmm(Field& f)
 		CCF_TRY(cudaGetLastError(), "star_hilo_kernel");
 	}
 
+	/* mean near-list length over the leaves (reported; the tracker's work per
+	   evaluation grows with it) */
+	{
+		std::vector<int> cnt(nl);
+		CCF_TRY(cudaMemcpyAsync(cnt.data(), f.leaf_near_count.ptr, nl * sizeof(int), cudaMemcpyDeviceToHost, s), "near counts");
+		CCF_TRY(cudaStreamSynchronize(s), "near counts");
+		double sum = 0;
+		for (int v : cnt) sum += v;
+		f.info.near_mean = nl > 0 ? sum / nl : 0;
+	}
+
 	/* smooth-mass polynomials */
 	float4 inv_corner_df = make_float4(0, 0, 0, 0);
 	SmoothPoly sp = smooth_polynomials(d.kappa_star, d.corner_x1, d.corner_x2, d.taylor_smooth);

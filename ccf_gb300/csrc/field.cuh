@@ -447,6 +447,25 @@ CCF_D float2 eval_df32(const FieldView& F, int leaf, double2 z, double2 s3_off)
 	return make_float2(-2 * t2 * s3.x - d2l.x - d2s.x, -2 * t2 * s3.y - d2l.y + d2s.y);
 }
 
+/* f'(z) for the mixed-precision solver: the FP32 evaluation, or FP64 where
+   that is not finite (far outside the field the smooth-mass Taylor terms
+   leave the FP32 range, and an infinite f' would make a zero step).
+   Off-field points take s3_off, the direct sum over every star. */
+CCF_D double2 eval_df_mixed(const FieldView& F, int leaf, double2 z, double2 s3_off)
+{
+	const float2 d = eval_df32(F, leaf, z, s3_off);
+	if (isfinite(d.x) && isfinite(d.y)) return make_double2(d.x, d.y);
+	double2 s3 = s3_off, d2l = make_double2(0, 0);
+	if (leaf >= 0)
+	{
+		s3 = leaf_sums<false, true>(F, leaf, z).s3;
+		const int P = F.order;
+		d2l = local_horner(F.leaf_loc + (size_t)leaf * 3 * (P + 1) + 2 * (P + 1), P, 3, leaf_dz(F, leaf, z));
+	}
+	const double2 d2s = smooth_d2zbar(F, z);
+	return make_double2(-2 * F.theta2 * s3.x - d2l.x - d2s.x, -2 * F.theta2 * s3.y - d2l.y + d2s.y);
+}
+
 /* everything the epilogue needs at a final root: the 1/mu error bound
    (ccf_functions.cuh:419-467), the caustic w = (1 - kappa) z + gamma zbar
    - alpha (ccf_functions.cuh:33-45) and the magnification length scale

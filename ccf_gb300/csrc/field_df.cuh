@@ -219,11 +219,11 @@ CCF_D TrackConst track_const(const FieldView& F)
    root inside the root box, from one pass over the leaf's near stars and one
    pair of Horner passes over its local expansion:
 
-     f      critical-curve function (double-float assembly, as eval_f_df), and
-            its FP32 rounding for the step;
-     df     f' in FP32 (as eval_df32);
-     pole   2 sum_i 1/(z - z_i) over the near stars (FP32), the Aberth
-            correction the tracker keeps;
+     step   f / (f' + f pole) in FP32, with f assembled in double-float (as
+            eval_f_df) and rounded, f' in FP32 (as eval_df32) and pole =
+            2 sum_i 1/(z - z_i) over the near stars (+ 2/z for the exact
+            disc), the part of the Aberth correction the tracker keeps;
+     fz, fs f in FP64 and f' step, for the 1/mu bound at the stepped root;
      wpart  the star, local and smooth-Taylor part of the lens map w
             (as eval_point_df): w = ((1 - kappa + gamma) x, (1 - kappa - gamma) y)
             + wpart, plus 2 kappa_star (corner.x + x) when wmode is 1 (the
@@ -237,19 +237,34 @@ CCF_D TrackConst track_const(const FieldView& F)
    centre in FP64; cph, sph = cos, sin phi. */
 struct TrackEval
 {
-	float2 f;
-	float2 df;
-	float2 pole;
-	dfc fd;
+	float2 step;      /* f / (f' + f pole) */
+	float as2;        /* |step|^2 */
+	double2 fz;       /* f in FP64 */
+	double af;        /* bound on |f| at the stepped root z - step: |f - f' step|,
+	                     the FP32 error of f' step, the double-float rounding of
+	                     the terms of f and the FP64 spacing of the root times |f'| */
 	dfc wpart;
 	int wmode;
 };
 
-CCF_D TrackEval eval_track_df(const FieldView& F, const TrackConst& K, int leaf, double2 z, double2 rel, dfl cph, dfl sph)
+/* a / b in FP32 with b scaled to unit size first, so that |b|^2 neither
+   overflows nor flushes to zero (a non-finite result marks a failed step) */
+CCF_D float2 fdiv_scaled(float2 a, float2 b)
+{
+	const float m = fmaxf(fabsf(b.x), fabsf(b.y));
+	const float im = 1.f / m;
+	const float bx = b.x * im, by = b.y * im, ax = a.x * im, ay = a.y * im;
+	const float r = 1.f / (bx * bx + by * by);
+	return make_float2((ax * bx + ay * by) * r, (ay * bx - ax * by) * r);
+}
+
+CCF_D TrackEval eval_track_df(const FieldView& F, const TrackConst& K, int leaf, double2 z, double2 rel, dfl cph, dfl sph,
+	bool disc_exact)
 {
 	const dfc zr = dfc_from(rel);
 	dfc s1 = {{0.f, 0.f}, {0.f, 0.f}}, s2 = s1;
 	float2 s3 = make_float2(0.f, 0.f), pole = make_float2(0.f, 0.f);
+	float tabs = 0.f;   /* sum of |m / d^2| */
 	const int n = F.leaf_near_count[leaf];
 	const float4* Pn = F.leaf_near_df + (size_t)leaf * MAX_NEAR;
 	const float2* Mn = F.leaf_mass_df + (size_t)leaf * MAX_NEAR;
@@ -276,6 +291,7 @@ CCF_D TrackEval eval_track_df(const FieldView& F, const TrackConst& K, int leaf,
 		const float i3y = i2x.hi * iy.hi + i2y.hi * ix.hi;        /* 1/d^3 */
 		s3.x = fmaf(m.hi, i3x, s3.x);
 		s3.y = fmaf(m.hi, i3y, s3.y);
+		tabs = fmaf(m.hi, fmaf(ix.hi, ix.hi, iy.hi * iy.hi), tabs);
 	}
 	const int P = F.order;
 	const float2 ihf = F.leaf_ih_df[leaf];
@@ -336,11 +352,28 @@ CCF_D TrackEval eval_track_df(const FieldView& F, const TrackConst& K, int leaf,
 	fi = df_add(fi, df_neg(dl.im));
 	fi = df_add(fi, ds.im);
 	fi = df_add(fi, df_mul(a, sph));
-	e.fd = {fr, fi};
-	e.f = make_float2(fr.hi + fr.lo, fi.hi + fi.lo);
+	e.fz = dfc_to({fr, fi});
+	const float2 f32 = make_float2(fr.hi + fr.lo, fi.hi + fi.lo);
 	const float t2 = K.theta2.hi;
-	e.df = make_float2(-2 * t2 * s3.x - d2l.x - d2s.x, -2 * t2 * s3.y - d2l.y + d2s.y);
-	e.pole = make_float2(2.f * pole.x, 2.f * pole.y);
+	const float2 df = make_float2(-2 * t2 * s3.x - d2l.x - d2s.x, -2 * t2 * s3.y - d2l.y + d2s.y);
+	pole = make_float2(2.f * pole.x, 2.f * pole.y);
+	if (disc_exact)
+	{
+		const float2 iz = finv(make_float2(zx, zy));
+		pole.x += 2.f * iz.x;
+		pole.y += 2.f * iz.y;
+	}
+	/* the step: f / (f' + f pole), FP32 */
+	const float2 st = fdiv_scaled(f32, fadd(df, fmulc(f32, pole)));
+	e.step = st;
+	e.as2 = st.x * st.x + st.y * st.y;
+	/* |f| at z - st: f - f' st (f holomorphic), the FP32 error of f' st, the
+	   double-float rounding of the terms of f (2^-47 of their sizes) and half
+	   the FP64 spacing of the root times |f'| */
+	const float2 fsv = fmulc(df, st);
+	const float terms = t2 * tabs + hypotf(dl.re.hi, dl.im.hi) + hypotf(ds.re.hi, ds.im.hi) + fabsf(a.hi) + fabsf(K.shear.hi);
+	e.af = hypot(e.fz.x - (double)fsv.x, e.fz.y - (double)fsv.y) +
+		(double)(1e-6f * hypotf(fsv.x, fsv.y) + 7.2e-15f * terms + 1.2e-16f * hypotf(zx, zy) * hypotf(df.x, df.y));
 	/* w - the linear terms: (-theta^2 s1.x - al.x - sa.x, theta^2 s1.y + al.y - sa.y) (eval_point_df) */
 	dfl wr = df_neg(df_mul(K.theta2, s1.re));
 	wr = df_add(wr, df_neg(al.re));

@@ -177,10 +177,10 @@ __device__ __noinline__ FdF eval_fdf_warp(const FieldView& F, bool valid, double
 	if (!valid) return r;
 	if constexpr (MIXED)
 	{
-		/* f in double-float on the FP32 pipe, off-field points included */
+		/* f in double-float on the FP32 pipe, off-field points included;
+		   f' in FP32, or FP64 where FP32 overflows */
 		r.f = eval_f_df(F, leaf, z, cphi, sphi, ns);
-		const float2 d32 = eval_df32(F, leaf, z, ns.s3);
-		r.df = make_double2(d32.x, d32.y);
+		r.df = eval_df_mixed(F, leaf, z, ns.s3);
 	}
 	else
 	{
@@ -574,7 +574,7 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 						}
 						else
 						{
-							fin[a] = 1;
+							fin[a] = 2;   /* frozen: counted as unconverged */
 							s_nan_step = 1;
 						}
 					}
@@ -629,7 +629,7 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 			const NearSums off = slot >= 0 ? s_offs[slot] : zero_sums();
 			if (!point_epilogue_warp<MIXED>(F, sO, v, z, leaf, slot >= 0, off, out, cphi, sphi, &s_maxerr)) s_nan_err = 1;
 			if (!v) continue;
-			if (!fin[a]) atomicAdd(&s_unconv, 1ull);
+			if (fin[a] != 1) atomicAdd(&s_unconv, 1ull);
 			if (initial)
 			{
 				long long cb = sR.cont_base;
@@ -703,6 +703,8 @@ constexpr int TNT = 128;                 /* threads per CTA of the tracker */
 constexpr int TSUB = 64;                 /* one phi step in sub-step units */
 constexpr int TRACK_ITERS = 6;           /* corrector iterations before the sub-step is halved */
 constexpr double TRACK_CONTRACT = 0.5;   /* each corrector step after the first must halve */
+constexpr double TRACK_CONTRACT_FINEST = 0.9;   /* ... or shrink by this at the finest sub-step */
+constexpr double TRACK_FS_REFINE = 1e-9;        /* bound on |f| above which a converged root takes one more step */
 constexpr int TABLE_PROBES = 64;         /* linear-probe bound of the column tables (load <= 1/2) */
 constexpr double CELL_PER_THETA = 1048576.0;   /* 2^20 cells per theta_star */
 
@@ -874,25 +876,41 @@ CCF_D void offfield_sums_warp_df(const FieldView& F, bool need, double2 z, NearS
 
 /* The iteration quantities of the tracker (TrackEval) for the warp's lanes
    with off set, which lie outside the root box: direct double-float sums over
-   every star, f, f' and the whole lens map (wmode 2) from the off-field
-   evaluators.  Kept out of line, as the rare path of the iteration.  All 32
-   lanes must call it. */
-__device__ __noinline__ TrackEval track_offfield(const FieldView& F, bool off, double2 z, double cphi, double sphi)
+   every star, then f, f', the step and the whole lens map (wmode 2) in FP64
+   (far from the field the smooth-mass Taylor terms leave the FP32 range).
+   Kept out of line, as the rare path of the iteration.  All 32 lanes must
+   call it. */
+__device__ __noinline__ TrackEval track_offfield(const FieldView& F, bool off, double2 z, double cphi, double sphi,
+	bool disc_exact)
 {
 	NearSums ns = zero_sums();
 	offfield_sums_warp_df<true, true>(F, off, z, ns);
 	TrackEval r;
-	r.f = make_float2(0.f, 0.f);
-	r.df = r.f;
-	r.pole = r.f;
-	r.fd = {{0.f, 0.f}, {0.f, 0.f}};
-	r.wpart = r.fd;
+	r.step = make_float2(0.f, 0.f);
+	r.as2 = 0;
+	r.fz = make_double2(0, 0);
+	r.af = 0;
+	r.wpart = {{0.f, 0.f}, {0.f, 0.f}};
 	r.wmode = 2;
 	if (!off) return r;
 	const double2 f = eval_f_df(F, -1, z, cphi, sphi, ns);
-	r.fd = dfc_from(f);
-	r.f = make_float2((float)f.x, (float)f.y);
-	r.df = eval_df32(F, -1, z, ns.s3);
+	const double2 df = eval_df_mixed(F, -1, z, ns.s3);
+	double2 S = make_double2(0, 0);
+	if (disc_exact)
+	{
+		const double2 iz = cinv(z);
+		S = make_double2(2 * iz.x, 2 * iz.y);
+	}
+	const double2 st = cdiv(f, cadd(df, cmul(f, S)));
+	r.step = make_float2((float)st.x, (float)st.y);
+	const double as2 = st.x * st.x + st.y * st.y;
+	r.as2 = as2 < 3e38 ? (float)as2 : INFINITY;   /* a step beyond the FP32 range fails */
+	r.fz = f;
+	const double2 fs = cmul(df, make_double2(r.step.x, r.step.y));
+	const double2 ds = smooth_dzbar(F, z);
+	r.af = hypot(f.x - fs.x, f.y - fs.y) +
+		7.2e-15 * (F.theta2 * hypot(ns.s2.x, ns.s2.y) + hypot(ds.x, ds.y) + 1 + F.shear) +
+		1.2e-16 * hypot(z.x, z.y) * hypot(df.x, df.y);
 	r.wpart = dfc_from(eval_point_df(F, -1, z, cphi, sphi, ns).w);
 	return r;
 }
@@ -904,17 +922,6 @@ CCF_D bool in_leaf_box(const FieldView& F, int leaf, double2 z, double2& rel)
 	rel = make_double2(z.x - c.x, z.y - c.y);
 	const double ih = F.leaf_inv_half[leaf];
 	return fabs(rel.x) * ih <= 1.0 && fabs(rel.y) * ih <= 1.0;
-}
-
-/* a / b in FP32 with b scaled to unit size first, so that |b|^2 neither
-   overflows nor flushes to zero (a non-finite result marks a failed step) */
-CCF_D float2 fdiv_scaled(float2 a, float2 b)
-{
-	const float m = fmaxf(fabsf(b.x), fabsf(b.y));
-	const float im = 1.f / m;
-	const float bx = b.x * im, by = b.y * im, ax = a.x * im, ay = a.y * im;
-	const float r = 1.f / (bx * bx + by * by);
-	return make_float2((ax * bx + ay * by) * r, (ay * bx - ax * by) * r);
 }
 
 CCF_D unsigned long long warp_sum_u64(unsigned long long v)
@@ -1111,6 +1118,10 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 		int it = 0, evs = 0;
 		double prev2 = 0;
 		bool lost = !valid;
+		bool refine = false;
+		/* corrector iterations per (sub-)step target: the sweep cap of the
+		   step, at most TRACK_ITERS (4 TRACK_ITERS at the finest sub-step) */
+		const int iters = min(TRACK_ITERS, cap), iters_finest = min(4 * TRACK_ITERS, cap);
 
 		while (__any_sync(full, act))
 		{
@@ -1125,32 +1136,22 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 			double2 step = make_double2(0, 0);
 			double as2 = 0;
 			TrackEval e;
-			e.f = make_float2(0.f, 0.f);
-			e.df = e.f;
-			e.pole = e.f;
-			e.fd = {{0.f, 0.f}, {0.f, 0.f}};
-			e.wpart = e.fd;
+			e.step = make_float2(0.f, 0.f);
+			e.as2 = 0;
+			e.fz = make_double2(0, 0);
+			e.af = 0;
+			e.wpart = {{0.f, 0.f}, {0.f, 0.f}};
 			e.wmode = 2;
 			if constexpr (MIXED)
 			{
-				if (act && leaf >= 0) e = eval_track_df(F, K, leaf, z, rel, cpd, spd);
+				if (act && leaf >= 0) e = eval_track_df(F, K, leaf, z, rel, cpd, spd, disc_exact);
 				if (__any_sync(full, off))
 				{
-					const TrackEval o = track_offfield(F, off, z, cp, sp);
+					const TrackEval o = track_offfield(F, off, z, cp, sp, disc_exact);
 					if (off) e = o;
 				}
-				if (act)
-				{
-					if (disc_exact)
-					{
-						const float2 iz = finv(make_float2((float)z.x, (float)z.y));
-						e.pole.x += 2.f * iz.x;
-						e.pole.y += 2.f * iz.y;
-					}
-					const float2 st = fdiv_scaled(e.f, fadd(e.df, fmulc(e.f, e.pole)));
-					step = make_double2((double)st.x, (double)st.y);
-					as2 = (double)(st.x * st.x + st.y * st.y);
-				}
+				step = make_double2((double)e.step.x, (double)e.step.y);
+				as2 = (double)e.as2;
 			}
 			else
 			{
@@ -1179,14 +1180,29 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 			{
 				nev++;
 				evs++;
+				/* at the finest sub-step the corrector may take linear steps (a
+				   pair of close zeros) as long as they keep shrinking */
+				const bool finest = tt - t1 <= 1;
+				const double contract = finest ? TRACK_CONTRACT_FINEST : TRACK_CONTRACT;
 				bool conv = false, fail = !isfinite(as2);
-				if (!fail && it > 0 && as2 >= tol2 && as2 > TRACK_CONTRACT * TRACK_CONTRACT * prev2) fail = true;
+				if (!fail && it > 0 && as2 >= tol2 && as2 > contract * contract * prev2) fail = true;
 				if (!fail)
 				{
 					it++;
 					prev2 = as2;
-					if (as2 < tol2) conv = true;
-					else if (it >= TRACK_ITERS) fail = true;
+					if (as2 < tol2)
+					{
+						conv = true;
+						/* a stiff root (large f' s, near a star): one more step from
+						   the stepped root, so that the 1/mu bound comes from an
+						   f evaluated there rather than from the first-order term */
+						if (!refine && !direct_out && tt == j * TSUB && e.af > TRACK_FS_REFINE)
+						{
+							conv = false;
+							refine = true;
+						}
+					}
+					else if (it >= (finest ? iters_finest : iters)) fail = true;
 				}
 				if (!fail) z = csub(z, step);
 				int tn = tt;
@@ -1203,6 +1219,7 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 					t1 = tt;
 					hz[0] = z1;
 					ht[0] = t1;
+					refine = false;
 					if (tt == j * TSUB)
 					{
 						emit = true;
@@ -1234,14 +1251,11 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 									}
 								}
 								const double av = 1 - F.kappa_tot - smooth_dz(F, ze);
-								const double2 fz = dfc_to(e.fd);
+								const double2 fz = e.fz;
 								const double gx = fz.x + av * cp, gy = -fz.y + av * sp;
 								wv.x -= av * step.x + gx * step.x + gy * step.y;
 								wv.y -= av * step.y - gx * step.y + gy * step.x;
-								/* f at zf: f(ze) - f' s, with a bound on the FP32 error of f' s */
-								const float2 fs = fmulc(e.df, make_float2((float)step.x, (float)step.y));
-								const double fx = fz.x - (double)fs.x, fy = fz.y - (double)fs.y;
-								const double af = hypot(fx, fy) + 1e-6 * (double)hypotf(fs.x, fs.y);
+								const double af = e.af;
 								const double err = fmax(fabs(af * (af + 2 * av)), fabs(af * (af - 2 * av)));
 								O.ccs[out] = zf;
 								O.errs[out] = err;
@@ -1265,6 +1279,7 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 				}
 				else if (fail)
 				{
+					refine = false;
 					if (tt - t1 > 1)
 					{
 						tn = t1 + (tt - t1) / 2;
@@ -1276,8 +1291,10 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 						act = false;
 					}
 				}
-				if (act && evs >= cap)
+				if (act && evs >= cap * TSUB)
 				{
+					/* a bound on the evaluations of one phi step (sub-steps
+					   included), so that the loop ends whatever the field */
 					lost = true;
 					act = false;
 				}

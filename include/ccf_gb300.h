@@ -159,7 +159,8 @@ typedef struct ccf_info
 	long long rerun_flags;       /* why rows were re-run: 1 two roots on one zero, 2 a
 	                                root lost, 4 a non-finite 1/mu bound, 8 a full
 	                                column table (bits OR-ed over the rows) */
-	double reserved[2];
+	double near_mean;            /* mean number of stars in a leaf's near list */
+	double reserved[1];
 } ccf_info;
 
 typedef struct ccf_handle ccf_handle;
