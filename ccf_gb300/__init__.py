@@ -4,6 +4,6 @@ The computation lives in the native library built from ``ccf_gb300/csrc``
 (CUDA kernels for sm_103a behind the C ABI of ``include/ccf_gb300.h``);
 this package is a thin Python front end over that ABI.
 """
-from .ccf import CCF, BatchJob, CCFError, Server, derive_params, run_batch, submit_batch  # noqa: F401
+from .ccf import CCF, BatchJob, CCFError, Server, derive_params, pinned_empty, run_batch, submit_batch  # noqa: F401
 
-__all__ = ["CCF", "BatchJob", "CCFError", "Server", "derive_params", "run_batch", "submit_batch"]
+__all__ = ["CCF", "BatchJob", "CCFError", "Server", "derive_params", "pinned_empty", "run_batch", "submit_batch"]

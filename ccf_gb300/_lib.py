@@ -124,7 +124,7 @@ EXPORTED = [
     "ccf_continue_branch_noalloc", "ccf_estimate_device_bytes", "ccf_batch_submit", "ccf_batch_poll",
     "ccf_batch_wait", "ccf_batch_destroy", "ccf_server_create", "ccf_server_submit", "ccf_server_wait",
     "ccf_server_request_info", "ccf_server_handle", "ccf_server_release", "ccf_server_get_stats",
-    "ccf_server_destroy",
+    "ccf_server_destroy", "ccf_host_alloc", "ccf_host_free",
 ]
 
 REQUEST_QUEUED, REQUEST_RUNNING, REQUEST_DONE, REQUEST_FAILED, REQUEST_REJECTED = range(5)
@@ -209,6 +209,8 @@ def load(path: str | None = None):
         L.ccf_get_device_results.argtypes = [H] + [ctypes.POINTER(ctypes.c_void_p)] * 4
         L.ccf_last_error.argtypes = [H]
         L.ccf_last_error.restype = ctypes.c_char_p
+        L.ccf_host_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]
+        L.ccf_host_free.argtypes = [ctypes.c_void_p]
         L.ccf_derive_params.argtypes = [PP, PI, ctypes.c_char_p, ctypes.c_size_t]
         L.ccf_run_batch.argtypes = [ctypes.POINTER(H), ctypes.c_int, ctypes.c_int]
         L.ccf_write_star_file.argtypes = [H, ctypes.c_char_p]

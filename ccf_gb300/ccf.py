@@ -11,6 +11,7 @@ and ``run_batch()`` to solve many fields in shared persistent launches.
 from __future__ import annotations
 
 import ctypes
+import weakref
 
 import numpy as np
 
@@ -164,23 +165,56 @@ class CCF:
         self._L.ccf_get_info(self._h, ctypes.byref(i))
         return i.as_dict()
 
-    def results(self, stars: bool = True) -> dict:
+    def results(self, stars: bool = True, out: dict | None = None) -> dict:
         """Outputs in the reference's file layout: rows = num_roots * num_branches,
-        cols = num_phi / num_branches + 1, row = root * num_branches + branch."""
+        cols = num_phi / num_branches + 1, row = root * num_branches + branch.
+
+        out: arrays to fill instead of new ones ("ccs", "caustics", "errs",
+        "mu_length_scales", "stars"; C-contiguous, the shapes and dtypes of
+        the returned arrays), e.g. from result_buffers(pinned=True), whose
+        page-locked memory takes the device copies at full bandwidth."""
         inf = self.info()
         rows = inf["num_roots"] * self.num_branches
         cols = self.num_phi // self.num_branches + 1
-        ccs = np.empty((rows, cols), dtype=np.complex128)
-        errs = np.empty((rows, cols))
-        caus = np.empty((rows, cols), dtype=np.complex128) if self.write_caustics else None
-        mu = np.empty((rows, cols)) if self.write_mu_length_scales else None
-        st = np.empty((inf["num_stars"], 3)) if stars else None
+        out = out or {}
+
+        def buf(name, shape, dtype, want):
+            if not want:
+                return None
+            a = out.get(name)
+            if a is None:
+                return np.empty(shape, dtype=dtype)
+            if a.shape != shape or a.dtype != np.dtype(dtype) or not a.flags.c_contiguous:
+                raise ValueError(f"out[{name!r}] must be a C-contiguous {np.dtype(dtype)} array of shape {shape}")
+            return a
+
+        ccs = buf("ccs", (rows, cols), np.complex128, True)
+        errs = buf("errs", (rows, cols), np.float64, True)
+        caus = buf("caustics", (rows, cols), np.complex128, self.write_caustics)
+        mu = buf("mu_length_scales", (rows, cols), np.float64, self.write_mu_length_scales)
+        st = buf("stars", (inf["num_stars"], 3), np.float64, stars)
         dp = lambda a: None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
         rc = self._L.ccf_get_results(self._h, dp(ccs), dp(caus), dp(errs), dp(mu), dp(st))
         if rc != 0:
             raise CCFError(rc, self.last_error())
         return {"ccs": ccs, "caustics": caus, "errs": errs, "mu_length_scales": mu, "stars": st, "info": inf}
 
+
+    def result_buffers(self, stars: bool = False, pinned: bool = True) -> dict:
+        """Arrays for results(out=...) sized for the current parameters (after
+        a run); page-locked when pinned."""
+        inf = self.info()
+        rows = inf["num_roots"] * self.num_branches
+        cols = self.num_phi // self.num_branches + 1
+        mk = pinned_empty if pinned else (lambda shape, dtype: np.empty(shape, dtype=dtype))
+        out = {"ccs": mk((rows, cols), np.complex128), "errs": mk((rows, cols), np.float64)}
+        if self.write_caustics:
+            out["caustics"] = mk((rows, cols), np.complex128)
+        if self.write_mu_length_scales:
+            out["mu_length_scales"] = mk((rows, cols), np.float64)
+        if stars:
+            out["stars"] = mk((inf["num_stars"], 3), np.float64)
+        return out
 
     def eval_points(self, z, phi) -> dict:
         """f, df/dz, lens map, 1/mu bound and length scale at points z (after run)."""
@@ -249,6 +283,23 @@ class BatchJob:
 def submit_batch(fields: list[CCF], verbose: int = 0) -> BatchJob:
     """run_batch without blocking: poll or wait on the returned job."""
     return BatchJob(fields, verbose)
+
+
+def pinned_empty(shape, dtype=np.float64) -> np.ndarray:
+    """An uninitialised array in page-locked host memory (ccf_host_alloc),
+    freed when the array is collected."""
+    L = _lib.load()
+    shape = tuple(int(x) for x in np.atleast_1d(shape))
+    dt = np.dtype(dtype)
+    nbytes = max(1, int(np.prod(shape)) * dt.itemsize)
+    p = ctypes.c_void_p()
+    rc = L.ccf_host_alloc(nbytes, ctypes.byref(p))
+    if rc != 0:
+        raise CCFError(rc, "ccf_host_alloc failed")
+    raw = (ctypes.c_char * nbytes).from_address(p.value)
+    weakref.finalize(raw, L.ccf_host_free, p.value)
+    a = np.frombuffer(raw, dtype=dt, count=int(np.prod(shape))).reshape(shape)
+    return a
 
 
 def _continuation_code(v) -> int:

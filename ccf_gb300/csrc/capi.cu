@@ -194,6 +194,31 @@ ccf_status ccf_get_device_results(ccf_handle* h, const double** ccs, const doubl
 	return CCF_OK;
 }
 
+ccf_status ccf_host_alloc(size_t bytes, void** out)
+{
+	if (!out) return CCF_ERR_INVALID_ARGUMENT;
+	*out = nullptr;
+	int n = 0;
+	if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0)
+	{
+		cudaGetLastError();
+		return CCF_ERR_NO_DEVICE;
+	}
+	if (cudaHostAlloc(out, bytes > 0 ? bytes : 1, cudaHostAllocDefault) != cudaSuccess)
+	{
+		cudaGetLastError();
+		*out = nullptr;
+		return CCF_ERR_OUT_OF_MEMORY;
+	}
+	return CCF_OK;
+}
+
+ccf_status ccf_host_free(void* p)
+{
+	if (!p) return CCF_OK;
+	return cudaFreeHost(p) == cudaSuccess ? CCF_OK : CCF_ERR_CUDA;
+}
+
 const char* ccf_last_error(const ccf_handle* h)
 {
 	if (!h) return "null handle";

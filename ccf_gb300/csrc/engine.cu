@@ -663,7 +663,7 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 	if (track)
 	{
 		CCF_TRY(P.track_table.ensure(table_slots), "cudaMalloc(tables)");
-		CCF_TRY(P.row_stats.ensure(3 * rc.size()), "cudaMalloc(rows)");
+		CCF_TRY(P.row_stats.ensure(TRACK_ROW_STATS * rc.size()), "cudaMalloc(rows)");
 		CCF_TRY(P.rows_rerun.ensure(rc.size()), "cudaMalloc(rows)");
 		CCF_TRY(P.rerun_count.ensure(3), "cudaMalloc(rows)");
 		CCF_TRY(P.item_start.ensure(rc.size()), "cudaMalloc(rows)");
@@ -735,7 +735,7 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		T.is_solo = P.is_solo.ptr;
 		CCF_TRY(cudaMemsetAsync(T.num_solo, 0, sizeof(int), s), "memset");
 		CCF_TRY(cudaMemsetAsync(P.track_table.ptr, 0, table_slots * sizeof(unsigned long long), s), "memset");
-		CCF_TRY(cudaMemsetAsync(P.row_stats.ptr, 0, 3 * rc.size() * sizeof(unsigned long long), s), "memset");
+		CCF_TRY(cudaMemsetAsync(P.row_stats.ptr, 0, TRACK_ROW_STATS * rc.size() * sizeof(unsigned long long), s), "memset");
 		CCF_TRY(cudaMemsetAsync(P.rerun_count.ptr, 0, 3 * sizeof(int), s), "memset");
 		CCF_TRY(launch_track_mark(s, T), "track_mark");
 		CCF_TRY(launch_track(s, T, mixed), "track_ccs");

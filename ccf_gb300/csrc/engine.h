@@ -138,7 +138,7 @@ struct SolverPools
 	DBuf<double2> fval_init, fval_cont;   /* f, f' per root */
 	DBuf<RowDesc> rows_init, rows_cont, rows_rerun;
 	DBuf<unsigned long long> track_table;   /* column tables of the tracker */
-	DBuf<unsigned long long> row_stats;     /* 3 per continuation row */
+	DBuf<unsigned long long> row_stats;     /* TRACK_ROW_STATS per continuation row */
 	DBuf<int> rerun_count;                  /* [0] rows to re-run, [1] [2] tracker work counters */
 	DBuf<int> item_start;                   /* first tracker work item of each continuation row */
 	DBuf<int2> solo;                        /* tracker roots run alone, and their count after them */

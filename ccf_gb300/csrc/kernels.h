@@ -95,9 +95,10 @@ struct SolveArgs
 };
 
 /* Per-root tracking of the continuation rows (solver.cu, track_kernel).
-   Row statistics: [3 row + 0] largest 1/mu bound (double bits), [3 row + 1]
-   TRACK_* flags, [3 row + 2] most evaluations one root needed for one phi
-   step. */
+   Row statistics, TRACK_ROW_STATS per row: [0] largest 1/mu bound (double
+   bits), [1] TRACK_* flags, [2] most evaluations one root needed for one phi
+   step, [3] points kept unconverged (the corrector stalled next to a zero). */
+constexpr int TRACK_ROW_STATS = 4;
 constexpr unsigned long long TRACK_DUPLICATE = 1;    /* two roots of a column on one zero */
 constexpr unsigned long long TRACK_LOST = 2;         /* a root that did not converge */
 constexpr unsigned long long TRACK_NONFINITE = 4;    /* a non-finite 1/mu bound */
@@ -111,7 +112,7 @@ struct TrackArgs
 	int num_rows;
 	const double2* master;      /* start roots (the branch centre), master[row.base + root]; read only */
 	unsigned long long* table;  /* column tables: 2 R slots per phi step, zeroed before the launch */
-	unsigned long long* row_stats;   /* 3 per row, zeroed before the launch */
+	unsigned long long* row_stats;   /* TRACK_ROW_STATS per row, zeroed before the launch */
 	const int* item_start;      /* [num_rows]: first work item (32 roots) of each row */
 	int num_items;
 	int* counter;               /* [0] next solo root, [1] next item in order; zeroed before the launch */

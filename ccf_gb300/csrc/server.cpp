@@ -47,8 +47,9 @@ unsigned long long estimate_bytes(const ccf_params& p, const ccf::Derived& d)
 	b += nodes * (32 * 32 + 3 * P1 * 16 + P1 * 8 + 32 * 24 + 2 * P1 * 16 + 64);
 	/* solver rows: centres and (branch, side) rows, 69 bytes per root */
 	b += 3 * nb * R * 69;
-	/* tracker: column tables, 2 R slots of 8 bytes per phi step of every row */
-	if (p.continuation == CCF_CONTINUATION_TRACK) b += 2 * nb * (cols / 2) * 2 * R * 8 + 2 * nb * (24 + 40);
+	/* tracker: column tables (2 R slots of 8 bytes per phi step of every row),
+	   solo-root lists (9 bytes per root of a row), row records and statistics */
+	if (p.continuation == CCF_CONTINUATION_TRACK) b += 2 * nb * (cols / 2) * 2 * R * 8 + 2 * nb * R * 9 + 2 * nb * (40 + 40);
 	/* outputs in the file layout */
 	const unsigned long long pts = R * nb * cols;
 	b += pts * (16 + 8);

@@ -704,8 +704,11 @@ constexpr int TSUB = 64;                 /* one phi step in sub-step units */
 constexpr int TRACK_ITERS = 6;           /* corrector iterations before the sub-step is halved */
 constexpr double TRACK_CONTRACT = 0.5;   /* each corrector step after the first must halve */
 constexpr double TRACK_CONTRACT_FINEST = 0.9;   /* ... or shrink by this at the finest sub-step */
+constexpr double TRACK_STUCK = 1e-6;            /* theta_star: a root whose corrector stalls at the finest
+                                                   sub-step with steps below this is kept, as unconverged */
 constexpr double TRACK_FS_REFINE = 1e-9;        /* bound on |f| above which a converged root takes one more step */
-constexpr int TABLE_PROBES = 64;         /* linear-probe bound of the column tables (load <= 1/2) */
+constexpr int TABLE_PROBES = 1024;       /* linear-probe bound of the column tables (load <= 1/2: the
+                                            longest cluster of a table of 1e5 slots is ~60) */
 constexpr double CELL_PER_THETA = 1048576.0;   /* 2^20 cells per theta_star */
 
 /* 2 sum_i 1/(z - z_i) over the near stars of the leaf; zero off the root box.
@@ -1119,6 +1122,7 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 		double prev2 = 0;
 		bool lost = !valid;
 		bool refine = false;
+		unsigned unconv = 0;
 		/* corrector iterations per (sub-)step target: the sweep cap of the
 		   step, at most TRACK_ITERS (4 TRACK_ITERS at the finest sub-step) */
 		const int iters = min(TRACK_ITERS, cap), iters_finest = min(4 * TRACK_ITERS, cap);
@@ -1205,6 +1209,17 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 					else if (it >= (finest ? iters_finest : iters)) fail = true;
 				}
 				if (!fail) z = csub(z, step);
+				if (fail && finest && isfinite(as2) && as2 < TRACK_STUCK * TRACK_STUCK * F.theta * F.theta)
+				{
+					/* the corrector stalls next to a zero (the function is only as
+					   smooth as its evaluation: neighbouring leaf expansions meet
+					   with a small jump), as the full Aberth step does there: keep
+					   the position as this target's root and count it unconverged,
+					   as the reference counts a root that reaches its sweep cap */
+					fail = false;
+					conv = true;
+					if (tt == j * TSUB) unconv++;
+				}
 				int tn = tt;
 				if (conv)
 				{
@@ -1324,6 +1339,7 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 			}
 		}
 		if (valid && lost) flags |= (unsigned)TRACK_LOST;
+		unconv = __reduce_add_sync(full, unconv);
 		flags = __reduce_or_sync(full, flags);
 		maxev = (int)__reduce_max_sync(full, (unsigned)maxev);
 		nev = warp_sum_u64(nev);
@@ -1331,10 +1347,11 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 		__syncwarp();
 		if (lane == 0)
 		{
-			unsigned long long* rs = T.row_stats + 3 * (size_t)row;
+			unsigned long long* rs = T.row_stats + TRACK_ROW_STATS * (size_t)row;
 			atomicMax(&rs[0], (unsigned long long)__double_as_longlong(s_maxerr[w]));
 			if (flags) atomicOr(&rs[1], (unsigned long long)flags);
 			atomicMax(&rs[2], (unsigned long long)maxev);
+			if (unconv) atomicAdd(&rs[3], (unsigned long long)unconv);
 			atomicAdd(&O.stats[2], nev);
 			if (nhalf) atomicAdd(&O.stats[10], nhalf);
 		}
@@ -1342,13 +1359,14 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 }
 
 /* Rows the tracker flagged go to the re-run list (and count in stats[9]);
-   the others report their largest 1/mu bound and evaluations per step. */
+   the others report their largest 1/mu bound, evaluations per step and
+   unconverged points. */
 __global__ void collect_rerun_kernel(const TrackArgs T, RowDesc* rerun, int* count)
 {
 	const int r = blockIdx.x * blockDim.x + threadIdx.x;
 	if (r >= T.num_rows) return;
 	const RowDesc row = T.rows[r];
-	const unsigned long long* rs = T.row_stats + 3 * (size_t)r;
+	const unsigned long long* rs = T.row_stats + TRACK_ROW_STATS * (size_t)r;
 	unsigned long long* st = T.outs[row.field].stats;
 	if (rs[1])
 	{
@@ -1361,6 +1379,7 @@ __global__ void collect_rerun_kernel(const TrackArgs T, RowDesc* rerun, int* cou
 	{
 		atomicMax(&st[0], rs[0]);
 		atomicMax(&st[6], rs[2]);
+		if (rs[3]) atomicAdd(&st[4], rs[3]);
 	}
 }
 

@@ -213,6 +213,13 @@ ccf_status ccf_get_results(ccf_handle* h, double* ccs, double* caustics, double*
 ccf_status ccf_get_device_results(ccf_handle* h, const double** ccs, const double** caustics,
 	const double** errs, const double** mu_length_scales);
 
+/* Page-locked host memory for the destinations of ccf_get_results (copies
+   into it run at the full host-device bandwidth; pageable destinations are
+   staged).  An addition of this library, with no counterpart in the
+   reference.  CCF_ERR_NO_DEVICE without a CUDA device. */
+ccf_status ccf_host_alloc(size_t bytes, void** out);
+ccf_status ccf_host_free(void* p);
+
 /* Message of the last failure on this handle ("" if none). */
 const char* ccf_last_error(const ccf_handle* h);
 

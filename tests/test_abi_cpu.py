@@ -151,3 +151,15 @@ def test_continuation_parameter():
     assert derive_params(continuation="aberth")["rc"] == 0
     with pytest.raises(ValueError):
         derive_params(continuation="newton")
+
+
+def test_pinned_host_memory_needs_a_device():
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("checks the path without a GPU")
+    except ImportError:
+        pass
+    from ccf_gb300 import CCFError, pinned_empty
+    with pytest.raises(CCFError):
+        pinned_empty((4, 4))

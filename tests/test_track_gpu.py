@@ -86,3 +86,21 @@ def test_tracked_field_is_checked_and_deterministic():
     a = run(cfg, "aberth")
     m = O.match_sets(x["ccs"], a["ccs"], nb)
     assert m["non_bijective_cols"] == 0 and m["max_dist"] <= 1e-11
+
+
+def test_results_into_pinned_buffers():
+    from ccf_gb300 import pinned_empty
+    cfg = json.loads(str(np.load(GOLDEN[0])["params"]))
+    c = CCF(**cfg)
+    c.write_mu_length_scales = 0
+    assert c.run(-1), c.last_error()
+    a = c.results(stars=False)
+    bufs = c.result_buffers(pinned=True)
+    b = c.results(stars=False, out=bufs)
+    assert b["ccs"] is bufs["ccs"]
+    for k in ("ccs", "caustics", "errs"):
+        assert np.array_equal(a[k], b[k])
+    with pytest.raises(ValueError):
+        c.results(stars=False, out={"ccs": np.empty((3, 3), dtype=np.complex128)})
+    p = pinned_empty((5, 7), np.complex128)
+    assert p.shape == (5, 7) and p.dtype == np.complex128
