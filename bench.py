@@ -205,10 +205,10 @@ class ClockSampler:
 
 # DRAM bytes (read + write) of the continuation launch per continuation point,
 # from the ncu capture summarised in
-# profiles/track_kernel_n2000_salpeter_phi512.md: 94.4 MB for the 4056 * 512
+# profiles/track_kernel_n2000_salpeter_phi512.md: 89.2 MB for the 4056 * 512
 # continuation points of that launch (the 40-byte outputs and the column
 # tables; leaf records and stars stay in L2).  It grows with the points written.
-CONT_DRAM_BYTES_PER_POINT = 94.4e6 / (4056 * 512)
+CONT_DRAM_BYTES_PER_POINT = 89.2e6 / (4056 * 512)
 
 
 def hbm_peak_gbs() -> float | None:
@@ -407,7 +407,9 @@ def run_multi(args) -> None:
             span = reduce(r["span"], MAX)
             pts = reduce(float(r["points"]), SUM)
             lat = r["latency"]
-            sub = reqs[:args.fp64_requests]
+            # the plain-FP64 comparison replays the first requests of at most
+            # 5000 stars (a 50000-star field takes minutes in plain FP64)
+            sub = [q for q in reqs if q[1]["num_stars"] <= 5000][:args.fp64_requests]
             r64 = stream("fp64", sub)
             rm = stream("mixed", sub)
             line.update({"value": pts / span, "ms_per_step": 1e3 * span, "steps": 1, "scaling": "weak",

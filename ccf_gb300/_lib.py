@@ -55,7 +55,8 @@ class CcfParams(ctypes.Structure):
         ("exact_binomials", ctypes.c_int),
         ("device", ctypes.c_int),
         ("continuation", ctypes.c_int),
-        ("reserved", ctypes.c_int * 7),
+        ("solved_centres", ctypes.c_int),
+        ("reserved", ctypes.c_int * 6),
     ]
 
 
@@ -109,7 +110,8 @@ class CcfInfo(ctypes.Structure):
         ("step_halvings", ctypes.c_longlong),
         ("rerun_flags", ctypes.c_longlong),
         ("near_mean", ctypes.c_double),
-        ("reserved", ctypes.c_double * 1),
+        ("centres_solved", ctypes.c_int),
+        ("reserved_int", ctypes.c_int),
     ]
 
     def as_dict(self) -> dict:

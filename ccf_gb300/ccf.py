@@ -68,6 +68,7 @@ class CCF:
         self.exact_binomials = 0
         self.device = 0
         self.continuation = "track"
+        self.solved_centres = 0
         self._stars_keep = None
         self.last_status = 0
         for k, v in kw.items():
@@ -104,6 +105,7 @@ class CCF:
         p.exact_binomials = int(self.exact_binomials)
         p.device = int(self.device)
         p.continuation = _continuation_code(self.continuation)
+        p.solved_centres = int(self.solved_centres)
         return p
 
     def _push(self):
@@ -324,6 +326,7 @@ def _bare(**kw) -> CCF:
     c.precision, c.output_float, c.max_iters_init, c.max_iters_step, c.exact_binomials, c.device = \
         "mixed", 0, 300, 60, 0, 0
     c.continuation = "track"
+    c.solved_centres = 0
     c._stars_keep = None
     c.last_status = 0
     for k, v in kw.items():

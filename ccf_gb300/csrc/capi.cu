@@ -64,6 +64,7 @@ void ccf_default_params(ccf_params* p)
 	p->exact_binomials = 0;
 	p->device = 0;
 	p->continuation = CCF_CONTINUATION_TRACK;
+	p->solved_centres = 0;
 }
 
 ccf_status ccf_create(ccf_handle** out)

@@ -526,6 +526,9 @@ static size_t nb_total(const std::vector<Field*>& fields)
 	return n;
 }
 
+/* largest number of branches per solved centre the engine picks by itself */
+constexpr int MAX_SEG = 16;
+
 ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 {
 	cudaStream_t s = stream;
@@ -545,6 +548,30 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 			return CCF_ERR_INVALID_ARGUMENT;
 		}
 	}
+	/* Solved centres: with the full-sum continuation every branch centre, as
+	   the reference.  With the tracker, every seg-th centre, seg the largest
+	   divisor of num_branches up to 16 that still gives the continuation about
+	   two resident waves of tracked roots (2 rows of R roots per centre): the
+	   initial solve costs O(R (R + N)) per sweep and centre, the tracker only
+	   its evaluations, and rows from a centre then cover seg branches.  The cap
+	   bounds the chain of a root that starts off the root box, which one warp
+	   tracks alone with direct star sums (on the 20000-star field 8 of 128
+	   centres take 0.62 s per field, 2 centres 3.2 s, all 128 1.50 s). */
+	const long long lanes_wanted = 2LL * num_sms * 16 * 32;
+	std::vector<int> seg(nf);
+	for (int i = 0; i < nf; i++)
+	{
+		const int R = fields[i]->d.num_roots, nb = fields[i]->params.num_branches;
+		seg[i] = 1;
+		if (track && fields[i]->params.solved_centres > 0) seg[i] = nb / fields[i]->params.solved_centres;
+		else if (track)
+			for (int g = std::min(nb, MAX_SEG); g > 1; g--)
+				if (nb % g == 0 && 2LL * (nb / g) * R >= lanes_wanted)
+				{
+					seg[i] = g;
+					break;
+				}
+	}
 	/* row offsets */
 	std::vector<long long> init_off(nf), cont_off(nf);
 	long long ninit = 0, ncont = 0;
@@ -552,12 +579,13 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 	for (int i = 0; i < nf; i++)
 	{
 		const int R = fields[i]->d.num_roots, nb = fields[i]->params.num_branches;
+		const int K = nb / seg[i];
 		init_off[i] = ninit;
 		cont_off[i] = ncont;
-		ninit += (long long)nb * R;
-		ncont += (long long)2 * nb * R;
-		rows_init += nb;
-		rows_cont += 2 * nb;
+		ninit += (long long)K * R;
+		ncont += (long long)2 * K * R;
+		rows_init += K;
+		rows_cont += 2 * K;
 		minR = std::min(minR, R);
 	}
 	SolverPools& P = pools;
@@ -605,36 +633,47 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		o.step_last = o.half;
 		o.max_iters_init = f.params.max_iters_init;
 		o.max_iters_step = f.params.max_iters_step;
+		o.seg = seg[i];
+		if (track)
+		{
+			CCF_TRY(f.phase.ensure(f.params.num_phi), "cudaMalloc(phase)");
+			CCF_TRY(launch_phase_table(s, nb, f.params.num_phi, f.phase.ptr), "phase_table_kernel");
+			o.phase = f.phase.ptr;
+		}
 		o.cont_master = P.master_cont.ptr;
 		o.cont_snap32 = mixed ? P.snap32_cont.ptr : nullptr;
 		o.cont_snap64 = mixed ? nullptr : P.snap64_cont.ptr;
 		o.stats = f.stats.ptr;
 		hilo[i] = mixed ? f.star_hilo.ptr : nullptr;
 		double cost = (double)R * (double)(R + N);
-		for (int c = 0; c < nb; c++)
+		const int g = seg[i], K = nb / g;
+		for (int q = 0; q < K; q++)
 		{
 			RowDesc r;
 			r.field = i;
-			r.branch = c;
+			r.branch = q * g;
 			r.side = -1;
-			r.pad = 0;
-			r.base = init_off[i] + (long long)c * R;
-			r.cont_base = cont_off[i] + (long long)(2 * c) * R;
+			r.steps = 0;
+			r.base = init_off[i] + (long long)q * R;
+			r.cont_base = cont_off[i] + (long long)(2 * q) * R;
 			ri.push_back(r);
 			cost_i.push_back(cost);
 			for (int b = 0; b < 2; b++)
 			{
-				RowDesc q = r;
-				q.side = b;
-				q.base = cont_off[i] + (long long)(2 * c + b) * R;
-				q.cont_base = table_slots;
-				table_slots += 2LL * R * (o.step_last - o.step_first + 1);
-				rc.push_back(q);
-				cost_c.push_back(cost * o.half);
+				RowDesc u = r;
+				u.side = b;
+				/* side 1 reaches half way to the next solved centre; side 0 stops
+				   one step short of it unless every centre is solved (row_slots) */
+				u.steps = g == 1 ? o.half : (b == 1 ? g * o.half : g * o.half - 1);
+				u.base = cont_off[i] + (long long)(2 * q + b) * R;
+				u.cont_base = table_slots;
+				table_slots += 2LL * R * u.steps;
+				rc.push_back(u);
+				cost_c.push_back(cost * u.steps);
 			}
 		}
-		/* seeds of every branch centre of this field */
-		launch_seed_roots(s, N, R, nb, f.star_gen.ptr, f.view.corner_abs, P.master_init.ptr + init_off[i],
+		/* seeds of the solved centres of this field */
+		launch_seed_roots(s, N, R, K, f.star_gen.ptr, f.view.corner_abs, P.master_init.ptr + init_off[i],
 			mixed ? P.snap32_init.ptr + init_off[i] : nullptr, mixed ? nullptr : P.snap64_init.ptr + init_off[i]);
 	}
 	/* largest rows first */
@@ -673,7 +712,7 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 	const int slots = num_sms * slots_per_sm;
 	auto pick_cluster = [&](int rows) {
 		int cl = 1;
-		while (cl < 8 && (long long)rows * cl * 2 <= slots && minR / (cl * 2) >= 256) cl *= 2;
+		while (cl < 16 && (long long)rows * cl * 2 <= slots && minR / (cl * 2) >= 256) cl *= 2;
 		return cl;
 	};
 	SolveArgs A;
@@ -748,8 +787,9 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 	CCF_TRY(cudaStreamSynchronize(s), "solver");
 
 	ccf_status status = CCF_OK;
-	for (Field* f : fields)
+	for (int fi = 0; fi < nf; fi++)
 	{
+		Field* f = fields[fi];
 		unsigned long long st[16];
 		CCF_TRY(cudaMemcpy(st, f->stats.ptr, 16 * sizeof(unsigned long long), cudaMemcpyDeviceToHost), "stats");
 		ccf_info& info = f->info;
@@ -773,10 +813,11 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		info.t_ccs = ev_ms(f->ev[4], f->ev[5]) * 1e-3;
 		info.t_caustics = 0;
 		info.t_total = ev_ms(f->ev[0], f->ev[5]) * 1e-3;
-		/* root seeds, initial solve, continuation (tracker: item marking,
-		   tracking, row collection and the full-sum launch for the rows to
-		   re-run) */
-		info.kernel_launches += track ? 6 : 3;
+		/* root seeds, initial solve, continuation (tracker: phase table, item
+		   marking, tracking, row collection and the full-sum launch for the
+		   rows to re-run) */
+		info.kernel_launches += track ? 7 : 3;
+		info.centres_solved = f->params.num_branches / seg[fi];
 		if (info.has_nan)
 		{
 			f->error = "Error. Errors in 1/mu contain values which are not positive real numbers.";

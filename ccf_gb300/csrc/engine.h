@@ -115,6 +115,9 @@ struct Field
 	FieldView view;
 	DBuf<FieldView> view_dev;
 
+	/* phase of every whole phi step (tracker) */
+	DBuf<PhaseEntry> phase;
+
 	/* outputs, file layout */
 	DBuf<double2> ccs, caustics;
 	DBuf<double> errs, mu;

@@ -38,15 +38,23 @@ struct TreeDev
 };
 
 /* one row of the root solver: all roots of one branch centre (initial
-   solve) or of one (branch, side) continuation */
+   solve) or of one (centre, side) continuation */
 struct RowDesc
 {
 	int field;         /* index into the launch's FieldView / FieldOut arrays */
-	int branch;        /* c */
+	int branch;        /* c, the branch whose centre the row starts from */
 	int side;          /* -1: initial solve at the branch centre; 0: phi decreasing; 1: increasing */
-	int pad;
+	int steps;         /* continuation rows: phi steps j = 1 .. steps (row_slots maps them to outputs) */
 	long long base;    /* offset of the row in master / snapshot / fin / list */
-	long long cont_base; /* initial rows: offset of the (branch, side 0) continuation row */
+	long long cont_base; /* initial rows: offset of the (branch, side 0) continuation row;
+	                        tracked continuation rows: offset of the row's column tables */
+};
+
+/* phase of a whole step of the phi grid: cos, sin in FP64 and double-float */
+struct PhaseEntry
+{
+	double2 cs;
+	float4 cs_df;      /* (cos hi, sin hi, cos lo, sin lo) */
 };
 
 /* per-field outputs and statistics of a solver launch */
@@ -64,6 +72,10 @@ struct FieldOut
 	int step_last;
 	int max_iters_init;
 	int max_iters_step;
+	int seg;               /* branches per solved centre: the initial solve runs at the centres
+	                          c = 0, seg, 2 seg, ... and the continuation rows from a centre cover
+	                          seg branches (1: every centre, the reference's scheme) */
+	const PhaseEntry* phase;   /* [nphi]: the phase of global step P (below) */
 	/* continuation arrays that the initial solve fills for both sides */
 	double2* cont_master;
 	float4* cont_snap32;
@@ -75,6 +87,53 @@ struct FieldOut
 	                                [9] continuation rows re-run by the full-sum solver, [10] tracker
 	                                sub-step halvings, [11] TRACK_* flags of the re-run rows */
 };
+
+/* Outputs of step j of the continuation row (c, side).  Global step
+   P = c 2 half +/- j (mod nphi) is the phase phi0 + P 2 pi / nphi; it is
+   column k = (P + half) mod 2 half of branch b = (P + half) / (2 half),
+   and at a branch boundary (k = 0) also column 2 half of branch b - 1 --
+   except the slot of the neighbouring solved centre's own row when every
+   centre is solved (seg = 1: the reference's layout, where row (c, 1) ends
+   in column 2 half of branch c and row (c + 1, 0) in column 0 of branch
+   c + 1).  Returns the number of slots (1 or 2) in b[], k[]. */
+CCF_HD int row_slots(int nb, int half, int seg, int c, int side, int j, int* b, int* k)
+{
+	const int period = 2 * half;
+	const int nphi = nb * period;
+	int P = c * period + (side ? j : -j);
+	P = ((P % nphi) + nphi) % nphi;
+	const int v = P + half;
+	int bb = v / period;
+	const int kk = v - bb * period;
+	bb %= nb;
+	int n = 0;
+	const int nbr = side ? (c + seg) % nb : (c - seg + nb) % nb;   /* the next solved centre that way */
+	if (!(kk == 0 && side == 1 && seg == 1 && bb == nbr))
+	{
+		b[n] = bb;
+		k[n] = kk;
+		n++;
+	}
+	if (kk == 0)
+	{
+		const int bp = (bb - 1 + nb) % nb;
+		if (!(side == 0 && seg == 1 && bp == nbr))
+		{
+			b[n] = bp;
+			k[n] = period;
+			n++;
+		}
+	}
+	return n;
+}
+
+/* global step of step j of row (c, side), in [0, nphi) */
+CCF_HD int row_global_step(int nb, int half, int c, int side, int j)
+{
+	const int nphi = nb * 2 * half;
+	const int P = c * 2 * half + (side ? j : -j);
+	return ((P % nphi) + nphi) % nphi;
+}
 
 struct SolveArgs
 {
@@ -157,6 +216,7 @@ void launch_leaf_df(cudaStream_t s, int num_leaves, int P, const double2* leaf_c
 int solver_blocks_per_sm(bool mixed);
 cudaError_t launch_solve(cudaStream_t s, const SolveArgs& a, bool mixed, bool initial);
 cudaError_t launch_track_mark(cudaStream_t s, const TrackArgs& a);
+cudaError_t launch_phase_table(cudaStream_t s, int nb, int nphi, PhaseEntry* out);
 cudaError_t launch_track(cudaStream_t s, const TrackArgs& a, bool mixed);
 cudaError_t launch_collect_rerun(cudaStream_t s, const TrackArgs& a, RowDesc* rerun, int* count);
 cudaError_t launch_eval_points(cudaStream_t s, const FieldView* F_dev, int npts, const double2* z, const double* phi,

@@ -126,6 +126,7 @@ extern "C" ccf_status ccf_continue_branch_noalloc(ccf_handle* h, int branch, int
 	o.half = half;
 	o.step_first = 1;
 	o.step_last = num_steps;
+	o.seg = 1;
 	o.max_iters_init = p.max_iters_init;
 	o.max_iters_step = p.max_iters_step;
 	o.stats = (unsigned long long*)(base + o_stats);
@@ -133,7 +134,7 @@ extern "C" ccf_status ccf_continue_branch_noalloc(ccf_handle* h, int branch, int
 	r.field = 0;
 	r.branch = branch;
 	r.side = side;
-	r.pad = 0;
+	r.steps = num_steps;
 	r.base = 0;
 	r.cont_base = 0;
 	const float4* hilo = mixed ? f.star_hilo.ptr : nullptr;

@@ -83,6 +83,11 @@ bool check_params(const ccf_params& p, bool star_input, std::string& msg)
 		msg = "Error. continuation must be 0 (track) or 1 (aberth).";
 		return false;
 	}
+	if (p.solved_centres < 0 || (p.solved_centres > 0 && (p.num_branches <= 0 || p.num_branches % p.solved_centres != 0)))
+	{
+		msg = "Error. solved_centres must be 0 or a divisor of num_branches.";
+		return false;
+	}
 	return true;
 }
 

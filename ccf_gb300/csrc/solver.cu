@@ -45,6 +45,7 @@ namespace ccf
 {
 
 constexpr int NT = 256;          /* threads per CTA */
+constexpr int MAX_CLUSTER = 16;  /* CTAs per row (above 8: the non-portable cluster sizes) */
 constexpr int TPT = 2;           /* targets per thread */
 constexpr int TILE = NT * TPT;   /* targets per tile */
 constexpr int CHUNK = 1024;      /* sources per shared-memory stage */
@@ -198,9 +199,11 @@ constexpr double STEP_TOL = 0.000000001;
    lanes must call it (see aberth_update_warp for leaf, have_off and off).
    With DF and no length scales every point is evaluated in double-float (off
    the root box from the star sums); length scales use FP64. */
+constexpr size_t NO_SLOT = ~(size_t)0;
+
 template <bool DF>
 __device__ __noinline__ bool point_epilogue_warp(const FieldView& F, const FieldOut& O, bool valid, double2 z, int leaf,
-	bool have_off, NearSums off, size_t out, double cphi, double sphi, double* maxerr)
+	bool have_off, NearSums off, size_t out, size_t out2, double cphi, double sphi, double* maxerr)
 {
 	NearSums ns = have_off ? off : zero_sums();
 	const bool mu = O.mu != nullptr;
@@ -218,6 +221,13 @@ __device__ __noinline__ bool point_epilogue_warp(const FieldView& F, const Field
 	O.errs[out] = pr.err;
 	if (O.caustics) O.caustics[out] = pr.w;
 	if (mu) O.mu[out] = pr.mu_length;
+	if (out2 != NO_SLOT)
+	{
+		O.ccs[out2] = z;
+		O.errs[out2] = pr.err;
+		if (O.caustics) O.caustics[out2] = pr.w;
+		if (mu) O.mu[out2] = pr.mu_length;
+	}
 	if (!isfinite(pr.err)) return false;
 	atomicMax((unsigned long long*)maxerr, (unsigned long long)__double_as_longlong(pr.err));
 	return true;
@@ -239,7 +249,7 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 	__shared__ RowDesc sR;
 	__shared__ int s_fill;
 	__shared__ int s_cnt;
-	__shared__ int s_pre[9];
+	__shared__ int s_pre[MAX_CLUSTER + 1];
 	__shared__ unsigned long long s_upd, s_terms, s_unconv;
 	__shared__ double s_maxerr;
 	__shared__ int s_nan_err, s_nan_step;   /* set by plain stores: every writer stores 1 */
@@ -273,7 +283,7 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 	const int o0 = (int)((long long)R * crank / csize);
 	const int o1 = (int)((long long)R * (crank + 1) / csize);
 	const int j0 = initial ? 0 : sO.step_first;
-	const int j1 = initial ? 0 : sO.step_last;
+	const int j1 = initial ? 0 : sR.steps;
 	const int max_it = initial ? sO.max_iters_init : sO.max_iters_step;
 	double2* __restrict__ master = A.master + base;
 	unsigned char* __restrict__ fin = A.fin + base;
@@ -601,7 +611,8 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 		sweeps_max = max(sweeps_max, it);
 
 		/* epilogue: outputs of this phi step for the roots this CTA owns */
-		const int k = initial ? sO.half : (side == 0 ? sO.half - j : sO.half + j);
+		int ob[2] = {c, c}, ok[2] = {sO.half, 0};
+		const int nslot = initial ? 1 : row_slots(nb, sO.half, sO.seg, c, side, j, ob, ok);
 		for (int a0 = o0; a0 < o1; a0 += NT)
 		{
 			/* uniform trip count: the epilogue is a warp-wide call */
@@ -625,9 +636,10 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 			const int K = min(s_noff, OFF_CAP);
 			if (sO.mu) offfield_sums_cta<MIXED, true, true>(F, s_offz, K, s_offs, red_off);
 			else offfield_sums_cta<MIXED, true, false>(F, s_offz, K, s_offs, red_off);
-			size_t out = ((size_t)(v ? a : 0) * nb + c) * sO.cols + k;
+			const size_t out = ((size_t)(v ? a : 0) * nb + ob[0]) * sO.cols + ok[0];
+			const size_t out2 = nslot > 1 ? ((size_t)(v ? a : 0) * nb + ob[1]) * sO.cols + ok[1] : NO_SLOT;
 			const NearSums off = slot >= 0 ? s_offs[slot] : zero_sums();
-			if (!point_epilogue_warp<MIXED>(F, sO, v, z, leaf, slot >= 0, off, out, cphi, sphi, &s_maxerr)) s_nan_err = 1;
+			if (!point_epilogue_warp<MIXED>(F, sO, v, z, leaf, slot >= 0, off, out, out2, cphi, sphi, &s_maxerr)) s_nan_err = 1;
 			if (!v) continue;
 			if (fin[a] != 1) atomicAdd(&s_unconv, 1ull);
 			if (initial)
@@ -974,32 +986,49 @@ __global__ void track_mark_kernel(const TrackArgs T)
 	}
 }
 
-/* phases of the whole steps of a row: cos, sin in FP64 and double-float */
-struct PhaseEntry
+/* cos, sin of sub-step position t of row (c, side): the field's phase table
+   for whole steps, else computed */
+CCF_D void track_phase(const FieldOut& O, int c, int side, int t, double& cp, double& sp, dfl& cpd, dfl& spd)
 {
-	double2 cs;
-	float4 cs_df;
-};
-constexpr int TRACK_TAB = 128;   /* whole steps per row held in shared memory */
-
-/* cos, sin of sub-step position t of a row: the table for whole steps, else
-   computed */
-CCF_D void track_phase(const PhaseEntry* tab, int tab_n, int c, int nb, int nphi, int side, int j0, int t, double& cp,
-	double& sp, dfl& cpd, dfl& spd)
-{
-	const int q = t / TSUB - (j0 - 1);
-	if (t % TSUB == 0 && q < tab_n)
+	if (t % TSUB == 0)
 	{
-		const PhaseEntry e = tab[q];
+		const PhaseEntry e = O.phase[row_global_step(O.nb, O.half, c, side, t / TSUB)];
 		cp = e.cs.x;
 		sp = e.cs.y;
 		cpd = {e.cs_df.x, e.cs_df.z};
 		spd = {e.cs_df.y, e.cs_df.w};
 		return;
 	}
-	sincos(track_phi(c, nb, nphi, side, t), &sp, &cp);
+	sincos(track_phi(c, O.nb, O.nphi, side, t), &sp, &cp);
 	cpd = df_from_double(cp);
 	spd = df_from_double(sp);
+}
+
+/* Phase of every whole step of a field's phi grid: global step P is the
+   phase row_phi gives for the branch centre nearest to it, so that with every
+   centre solved the tracker sees the same phases as the full-sum solver. */
+__global__ void phase_table_kernel(int nb, int nphi, PhaseEntry* out)
+{
+	const int P = blockIdx.x * blockDim.x + threadIdx.x;
+	if (P >= nphi) return;
+	const int period = nphi / nb, half = period / 2;
+	int c = (P + half) / period;
+	int u = P - c * period;            /* in [-half, half) */
+	c %= nb;
+	double sp, cp;
+	sincos(row_phi(c, nb, nphi, u < 0 ? 0 : 1, u < 0 ? -u : u), &sp, &cp);
+	const dfl cd = df_from_double(cp), sd = df_from_double(sp);
+	PhaseEntry e;
+	e.cs = make_double2(cp, sp);
+	e.cs_df = make_float4(cd.hi, sd.hi, cd.lo, sd.lo);
+	out[P] = e;
+}
+
+cudaError_t launch_phase_table(cudaStream_t s, int nb, int nphi, PhaseEntry* out)
+{
+	if (nphi <= 0) return cudaSuccess;
+	phase_table_kernel<<<(nphi + 127) / 128, 128, 0, s>>>(nb, nphi, out);
+	return cudaGetLastError();
 }
 
 /* A work item is 32 consecutive roots of one row, one warp; the rows of an
@@ -1029,12 +1058,10 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 	__shared__ double s_maxerr[TNT / 32];
 	__shared__ double2 s_hz[TRACK_HIST * TNT];   /* accepted positions of each lane's root, newest first */
 	__shared__ int s_ht[TRACK_HIST * TNT];
-	__shared__ PhaseEntry s_tab[TNT / 32][TRACK_TAB];
 	const unsigned full = 0xffffffffu;
 	const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	double2* const hz = s_hz + threadIdx.x;
 	int* const ht = s_ht + threadIdx.x;
-	PhaseEntry* const tab = s_tab[w];
 
 	while (true)
 	{
@@ -1080,7 +1107,7 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 		const int a = solo_root >= 0 ? solo_root : (item - T.item_start[row]) * 32 + lane;
 		const bool valid = solo_root >= 0 ? lane == 0 : (a < R && !T.is_solo[RD.base + a]);
 		const int c = RD.branch, side = RD.side, nb = O.nb, nphi = O.nphi;
-		const int j0 = O.step_first, j1 = O.step_last;
+		const int j0 = O.step_first, j1 = RD.steps;
 		const int cap = O.max_iters_step;
 		const double tol = STEP_TOL * F.theta;
 		const double tol2 = tol * tol;
@@ -1088,18 +1115,6 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 		const double inv_cell = CELL_PER_THETA / F.theta;
 		const unsigned long long slots = 2ull * (unsigned long long)R;
 		const bool direct_out = !MIXED || O.mu != nullptr;
-
-		/* phases of the row's whole steps j0 - 1 .. j1 */
-		const int tab_n = min(j1 - j0 + 2, TRACK_TAB);
-		for (int q = lane; q < tab_n; q += 32)
-		{
-			double sp, cp;
-			sincos(row_phi(c, nb, nphi, side, j0 - 1 + q), &sp, &cp);
-			const dfl cd = df_from_double(cp), sd = df_from_double(sp);
-			tab[q].cs = make_double2(cp, sp);
-			tab[q].cs_df = make_float4(cd.hi, sd.hi, cd.lo, sd.lo);
-		}
-		__syncwarp();
 
 		double2 z1 = valid ? T.master[RD.base + a] : make_double2(0, 0);
 		int t1 = (j0 - 1) * TSUB;
@@ -1117,7 +1132,7 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 		double2 z = z1;
 		double cp = 0, sp = 0;
 		dfl cpd = {0.f, 0.f}, spd = {0.f, 0.f};
-		track_phase(tab, tab_n, c, nb, nphi, side, j0, tt, cp, sp, cpd, spd);
+		track_phase(O, c, side, tt, cp, sp, cpd, spd);
 		int it = 0, evs = 0;
 		double prev2 = 0;
 		bool lost = !valid;
@@ -1178,7 +1193,7 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 			   here (mixed precision) or by the direct epilogue below */
 			bool emit = false;
 			double2 zf = make_double2(0, 0);
-			size_t out = 0;
+			size_t out = 0, out2 = NO_SLOT;
 			double ecp = 0, esp = 0;
 			if (act)
 			{
@@ -1241,8 +1256,10 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 						zf = z;
 						ecp = cp;
 						esp = sp;
-						const int k = side == 0 ? O.half - j : O.half + j;
-						out = ((size_t)a * nb + c) * O.cols + k;
+						int ob[2], ok[2];
+						const int nslot = row_slots(nb, O.half, O.seg, c, side, j, ob, ok);
+						out = ((size_t)a * nb + ob[0]) * O.cols + ok[0];
+						if (nslot > 1) out2 = ((size_t)a * nb + ob[1]) * O.cols + ok[1];
 						if constexpr (MIXED)
 						{
 							if (!direct_out)
@@ -1275,6 +1292,12 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 								O.ccs[out] = zf;
 								O.errs[out] = err;
 								if (O.caustics) O.caustics[out] = wv;
+								if (out2 != NO_SLOT)
+								{
+									O.ccs[out2] = zf;
+									O.errs[out2] = err;
+									if (O.caustics) O.caustics[out2] = wv;
+								}
 								if (isfinite(err)) atomicMax((unsigned long long*)&s_maxerr[w], (unsigned long long)__double_as_longlong(err));
 								else flags |= (unsigned)TRACK_NONFINITE;
 							}
@@ -1320,7 +1343,7 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 					z = track_predict(hz, ht, hn, tt);
 					it = 0;
 					prev2 = 0;
-					track_phase(tab, tab_n, c, nb, nphi, side, j0, tt, cp, sp, cpd, spd);
+					track_phase(O, c, side, tt, cp, sp, cpd, spd);
 				}
 			}
 
@@ -1334,7 +1357,7 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 					double2 r2;
 					leafo = (leaf >= 0 && in_leaf_box(F, leaf, zf, r2)) ? leaf : find_leaf(F, zf);
 				}
-				if (!point_epilogue_warp<MIXED>(F, O, emit_direct, zf, leafo, false, zero_sums(), out, ecp, esp, &s_maxerr[w]))
+				if (!point_epilogue_warp<MIXED>(F, O, emit_direct, zf, leafo, false, zero_sums(), out, out2, ecp, esp, &s_maxerr[w]))
 					flags |= (unsigned)TRACK_NONFINITE;
 			}
 		}
@@ -1429,6 +1452,18 @@ int solver_blocks_per_sm(bool mixed)
 cudaError_t launch_solve(cudaStream_t s, const SolveArgs& a, bool mixed, bool initial)
 {
 	if (a.num_rows == 0) return cudaSuccess;
+	if (a.cluster < 1 || a.cluster > MAX_CLUSTER) return cudaErrorInvalidValue;
+	if (a.cluster > 8)
+	{
+		static bool allowed[2] = {false, false};
+		if (!allowed[mixed ? 1 : 0])
+		{
+			cudaError_t e = mixed ? cudaFuncSetAttribute(solve_kernel<true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1)
+			                      : cudaFuncSetAttribute(solve_kernel<false>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+			if (e != cudaSuccess) return e;
+			allowed[mixed ? 1 : 0] = true;
+		}
+	}
 	cudaLaunchConfig_t cfg = {};
 	cfg.gridDim = dim3(a.num_rows * a.cluster, 1, 1);
 	cfg.blockDim = dim3(NT, 1, 1);

@@ -103,7 +103,10 @@ typedef struct ccf_params
 	                                0 (default): the reference's int32 table */
 	int device;                  /* CUDA device ordinal, default 0 */
 	int continuation;            /* ccf_continuation, default CCF_CONTINUATION_TRACK */
-	int reserved[7];
+	int solved_centres;          /* tracker: branch centres solved by the initial Aberth solve,
+	                                a divisor of num_branches (the others are reached by
+	                                tracking); 0 (default): as few as fill the GPU */
+	int reserved[6];
 } ccf_params;
 
 /* Derived parameters, statistics and timings of a run.  Names follow the keys
@@ -160,7 +163,9 @@ typedef struct ccf_info
 	                                root lost, 4 a non-finite 1/mu bound, 8 a full
 	                                column table (bits OR-ed over the rows) */
 	double near_mean;            /* mean number of stars in a leaf's near list */
-	double reserved[1];
+	int centres_solved;          /* branch centres solved by the initial Aberth solve (the
+	                                tracker solves every seg-th one and tracks the others) */
+	int reserved_int;
 } ccf_info;
 
 typedef struct ccf_handle ccf_handle;

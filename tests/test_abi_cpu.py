@@ -151,6 +151,10 @@ def test_continuation_parameter():
     assert derive_params(continuation="aberth")["rc"] == 0
     with pytest.raises(ValueError):
         derive_params(continuation="newton")
+    # solved centres: 0 (automatic) or a divisor of num_branches
+    assert derive_params(num_phi=64, num_branches=8, solved_centres=2)["rc"] == 0
+    d = derive_params(num_phi=64, num_branches=8, solved_centres=3)
+    assert d["rc"] != 0 and "solved_centres must be 0 or a divisor of num_branches" in d["error"]
 
 
 def test_pinned_host_memory_needs_a_device():

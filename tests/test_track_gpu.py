@@ -104,3 +104,21 @@ def test_results_into_pinned_buffers():
         c.results(stars=False, out={"ccs": np.empty((3, 3), dtype=np.complex128)})
     p = pinned_empty((5, 7), np.complex128)
     assert p.shape == (5, 7) and p.dtype == np.complex128
+
+
+@pytest.mark.parametrize("centres", [1, 2])
+def test_rows_across_branches_from_few_solved_centres(centres):
+    """Solving the initial roots at 1 or 2 of 4 branch centres and tracking the
+    others gives the zero sets of the full-sum continuation at every column."""
+    cfg = dict(kappa_tot=0.45, kappa_star=0.35, shear=0.35, mass_function="salpeter", m_lower=0.08, m_upper=1.5,
+               m_solar=4.954984, rectangular=1, approx=1, num_stars=300, num_phi=128, num_branches=4,
+               random_seed=91)
+    t = run(cfg, "track", solved_centres=centres)
+    a = run(cfg, "aberth")
+    assert t["info"]["centres_solved"] == centres
+    assert t["info"]["unconverged"] == 0
+    m = O.match_sets(t["ccs"], a["ccs"], cfg["num_branches"])
+    assert m["non_finite"] == 0 and m["non_bijective_cols"] == 0
+    assert m["max_dist"] <= 1e-11
+    mc = O.match_sets(t["caustics"], a["caustics"], cfg["num_branches"])
+    assert mc["max_dist"] <= 1e-10
