@@ -716,8 +716,11 @@ constexpr int TSUB = 64;                 /* one phi step in sub-step units */
 constexpr int TRACK_ITERS = 6;           /* corrector iterations before the sub-step is halved */
 constexpr double TRACK_CONTRACT = 0.5;   /* each corrector step after the first must halve */
 constexpr double TRACK_CONTRACT_FINEST = 0.9;   /* ... or shrink by this at the finest sub-step */
-constexpr double TRACK_STUCK = 1e-6;            /* theta_star: a root whose corrector stalls at the finest
-                                                   sub-step with steps below this is kept, as unconverged */
+constexpr double TRACK_STUCK = 1e-2;            /* theta_star: a root whose corrector stalls at the finest
+                                                   sub-step with steps below this is kept, as unconverged
+                                                   (the full Aberth step leaves such roots unconverged
+                                                   too: pairs of nearly coincident zeros); larger steps
+                                                   are a lost root and send the row to the re-run */
 constexpr double TRACK_FS_REFINE = 1e-9;        /* bound on |f| above which a converged root takes one more step */
 constexpr int TABLE_PROBES = 1024;       /* linear-probe bound of the column tables (load <= 1/2: the
                                             longest cluster of a table of 1e5 slots is ~60) */
@@ -1226,11 +1229,11 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 				if (!fail) z = csub(z, step);
 				if (fail && finest && isfinite(as2) && as2 < TRACK_STUCK * TRACK_STUCK * F.theta * F.theta)
 				{
-					/* the corrector stalls next to a zero (the function is only as
-					   smooth as its evaluation: neighbouring leaf expansions meet
-					   with a small jump), as the full Aberth step does there: keep
-					   the position as this target's root and count it unconverged,
-					   as the reference counts a root that reaches its sweep cap */
+					/* the corrector stalls next to a zero (nearly coincident zeros,
+					   or neighbouring leaf expansions meeting with a small jump in
+					   f), as the full Aberth step does there: keep the position as
+					   this target's root and count it unconverged, as the reference
+					   counts a root that reaches its sweep cap */
 					fail = false;
 					conv = true;
 					if (tt == j * TSUB) unconv++;
