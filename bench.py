@@ -410,8 +410,8 @@ def run_multi(args) -> None:
             # the plain-FP64 comparison replays the first requests of at most
             # 5000 stars (a 50000-star field takes minutes in plain FP64)
             sub = [q for q in reqs if q[1]["num_stars"] <= 5000][:args.fp64_requests]
-            r64 = stream("fp64", sub)
-            rm = stream("mixed", sub)
+            r64 = stream("fp64", sub) if sub else None
+            rm = stream("mixed", sub) if sub else None
             line.update({"value": pts / span, "ms_per_step": 1e3 * span, "steps": 1, "scaling": "weak",
                          "fields_per_s": reduce(float(len(reqs)), SUM) / span,
                          "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
@@ -426,7 +426,8 @@ def run_multi(args) -> None:
                          "server": dict(r["stats"]),
                          "fp64_plain": {"requests": len(sub), "value": r64["points"] / r64["span"],
                                         "mixed_same_requests": rm["points"] / rm["span"], "unit": "points/s",
-                                        "ratio_mixed_over_fp64": (rm["points"] / rm["span"]) / (r64["points"] / r64["span"])},
+                                        "ratio_mixed_over_fp64": (rm["points"] / rm["span"]) / (r64["points"] / r64["span"])}
+                         if sub else None,
                          "gpu_launches": None,
                          "detail": {"points": pts, "failed": r["failed"]}})
     line["clocks"] = clocks.summary()

@@ -111,7 +111,7 @@ class CcfInfo(ctypes.Structure):
         ("rerun_flags", ctypes.c_longlong),
         ("near_mean", ctypes.c_double),
         ("centres_solved", ctypes.c_int),
-        ("reserved_int", ctypes.c_int),
+        ("rows_retracked", ctypes.c_int),
     ]
 
     def as_dict(self) -> dict:

@@ -23,6 +23,8 @@ The engine never resets the device and reuses its buffers across runs.
 #include <cstdio>
 #include <cstring>
 #include <iostream>
+#include <map>
+#include <mutex>
 #include <numeric>
 
 namespace ccf
@@ -39,8 +41,57 @@ Field::~Field()
 {
 	if (events)
 	{
+		/* the buffers go back to the device-memory cache: wait for the last
+		   run's work on them first */
+		cudaEventSynchronize(ev[5]);
 		for (auto& e : ev) cudaEventDestroy(e);
 	}
+}
+
+namespace
+{
+std::mutex g_dmem_mutex;
+std::map<int, std::multimap<size_t, void*>> g_dmem;   /* device -> (bytes, block) */
+}
+
+cudaError_t dmem_alloc(void** p, size_t bytes, size_t* got)
+{
+	int dev = 0;
+	cudaGetDevice(&dev);
+	{
+		std::lock_guard<std::mutex> g(g_dmem_mutex);
+		auto& pool = g_dmem[dev];
+		auto it = pool.lower_bound(bytes);
+		/* a kept block of at most twice the size (and 1 MiB) */
+		if (it != pool.end() && it->first <= 2 * bytes + (1u << 20))
+		{
+			*p = it->second;
+			*got = it->first;
+			pool.erase(it);
+			return cudaSuccess;
+		}
+	}
+	cudaError_t e = cudaMalloc(p, bytes);
+	if (e == cudaErrorMemoryAllocation)
+	{
+		cudaGetLastError();
+		std::lock_guard<std::mutex> g(g_dmem_mutex);
+		for (auto& kv : g_dmem[dev]) cudaFree(kv.second);
+		g_dmem[dev].clear();
+		e = cudaMalloc(p, bytes);
+	}
+	if (e == cudaSuccess) *got = bytes;
+	return e;
+}
+
+void dmem_release(void* p, size_t bytes)
+{
+	int dev = 0;
+	cudaPointerAttributes a;
+	if (cudaPointerGetAttributes(&a, p) == cudaSuccess) dev = a.device;
+	else cudaGetLastError();
+	std::lock_guard<std::mutex> g(g_dmem_mutex);
+	g_dmem[dev].emplace(bytes, p);
 }
 
 TreeDev Field::tree_dev() const
@@ -68,7 +119,11 @@ Engine::Engine() {}
 
 Engine::~Engine()
 {
-	if (stream) cudaStreamDestroy(stream);
+	if (stream)
+	{
+		cudaStreamSynchronize(stream);   /* its pool buffers go back to the cache after this */
+		cudaStreamDestroy(stream);
+	}
 }
 
 ccf_status Engine::cuda_fail(cudaError_t e, const char* what)
@@ -575,7 +630,7 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 	/* row offsets */
 	std::vector<long long> init_off(nf), cont_off(nf);
 	long long ninit = 0, ncont = 0;
-	int rows_init = 0, rows_cont = 0, minR = 1 << 30;
+	int rows_init = 0, rows_cont = 0, minR = 1 << 30, maxR = 0;
 	for (int i = 0; i < nf; i++)
 	{
 		const int R = fields[i]->d.num_roots, nb = fields[i]->params.num_branches;
@@ -587,6 +642,7 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		rows_init += K;
 		rows_cont += 2 * K;
 		minR = std::min(minR, R);
+		maxR = std::max(maxR, R);
 	}
 	SolverPools& P = pools;
 	CCF_TRY(P.master_init.ensure(ninit), "cudaMalloc(roots)");
@@ -704,7 +760,9 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		CCF_TRY(P.track_table.ensure(table_slots), "cudaMalloc(tables)");
 		CCF_TRY(P.row_stats.ensure(TRACK_ROW_STATS * rc.size()), "cudaMalloc(rows)");
 		CCF_TRY(P.rows_rerun.ensure(rc.size()), "cudaMalloc(rows)");
-		CCF_TRY(P.rerun_count.ensure(3), "cudaMalloc(rows)");
+		CCF_TRY(P.rerun_count.ensure(6), "cudaMalloc(rows)");
+		CCF_TRY(P.rows_rerun2.ensure(rc.size()), "cudaMalloc(rows)");
+		CCF_TRY(P.row_stats2.ensure(TRACK_ROW_STATS * rc.size()), "cudaMalloc(rows)");
 		CCF_TRY(P.item_start.ensure(rc.size()), "cudaMalloc(rows)");
 	}
 
@@ -759,6 +817,9 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		T.row_stats = P.row_stats.ptr;
 		T.item_start = P.item_start.ptr;
 		T.counter = P.rerun_count.ptr + 1;
+		T.num_rows_dev = nullptr;
+		T.items_per_row = 0;
+		T.max_sub = TRACK_TSUB;
 		T.num_items = 0;
 		for (size_t r = 0; r < rc.size(); r++)
 		{
@@ -775,12 +836,28 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		CCF_TRY(cudaMemsetAsync(T.num_solo, 0, sizeof(int), s), "memset");
 		CCF_TRY(cudaMemsetAsync(P.track_table.ptr, 0, table_slots * sizeof(unsigned long long), s), "memset");
 		CCF_TRY(cudaMemsetAsync(P.row_stats.ptr, 0, TRACK_ROW_STATS * rc.size() * sizeof(unsigned long long), s), "memset");
-		CCF_TRY(cudaMemsetAsync(P.rerun_count.ptr, 0, 3 * sizeof(int), s), "memset");
+		CCF_TRY(cudaMemsetAsync(P.rerun_count.ptr, 0, 6 * sizeof(int), s), "memset");
+		CCF_TRY(cudaMemsetAsync(P.row_stats2.ptr, 0, TRACK_ROW_STATS * rc.size() * sizeof(unsigned long long), s), "memset");
 		CCF_TRY(launch_track_mark(s, T), "track_mark");
 		CCF_TRY(launch_track(s, T, mixed), "track_ccs");
 		CCF_TRY(launch_collect_rerun(s, T, P.rows_rerun.ptr, P.rerun_count.ptr), "collect_rerun");
-		A.rows = P.rows_rerun.ptr;
-		A.num_rows_dev = P.rerun_count.ptr;
+		/* rows that failed: tracked again from their centre with sub-steps of at
+		   most 1/TRACK_FINE_SUB of a phi step (the predictor's error falls as
+		   the fifth power of the step), then the rows failing still go to the
+		   full-sum solver; all on device-side row counts */
+		TrackArgs T2 = T;
+		T2.rows = P.rows_rerun.ptr;
+		T2.num_rows_dev = P.rerun_count.ptr;
+		T2.items_per_row = (maxR + 31) / 32;
+		T2.num_items = (int)rc.size() * T2.items_per_row;
+		T2.max_sub = TRACK_TSUB / TRACK_FINE_SUB;
+		T2.row_stats = P.row_stats2.ptr;
+		T2.counter = P.rerun_count.ptr + 4;
+		CCF_TRY(launch_clear_tables(s, T2), "clear_tables");
+		CCF_TRY(launch_track(s, T2, mixed), "track_ccs_fine");
+		CCF_TRY(launch_collect_rerun(s, T2, P.rows_rerun2.ptr, P.rerun_count.ptr + 3), "collect_rerun");
+		A.rows = P.rows_rerun2.ptr;
+		A.num_rows_dev = P.rerun_count.ptr + 3;
 	}
 	CCF_TRY(launch_solve(s, A, mixed, false), "find_ccs");
 	for (Field* f : fields) CCF_TRY(cudaEventRecord(f->ev[5], s), "event");
@@ -807,6 +884,7 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		info.rows_rerun = (long long)st[9];
 		info.step_halvings = (long long)st[10];
 		info.rerun_flags = (long long)st[11];
+		info.rows_retracked = (int)st[12];
 		info.t_stars = ev_ms(f->ev[0], f->ev[1]) * 1e-3;
 		info.t_tree = ev_ms(f->ev[1], f->ev[2]) * 1e-3;
 		info.t_init_roots = ev_ms(f->ev[3], f->ev[4]) * 1e-3;
@@ -814,9 +892,9 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		info.t_caustics = 0;
 		info.t_total = ev_ms(f->ev[0], f->ev[5]) * 1e-3;
 		/* root seeds, initial solve, continuation (tracker: phase table, item
-		   marking, tracking, row collection and the full-sum launch for the
-		   rows to re-run) */
-		info.kernel_launches += track ? 7 : 3;
+		   marking, tracking, row collection, table clearing, re-tracking, row
+		   collection and the full-sum launch for the rows to re-run) */
+		info.kernel_launches += track ? 10 : 3;
 		info.centres_solved = f->params.num_branches / seg[fi];
 		if (info.has_nan)
 		{

@@ -16,6 +16,17 @@ CCF<T>::run / save, include/ccf.cuh:1265-1287) and of batches of fields.
 namespace ccf
 {
 
+/* Device memory for DBuf: blocks that a released buffer gave back are kept
+   per device and handed to later buffers of a fitting size instead of going
+   through cudaFree, which synchronises the whole device -- with several
+   requests running on their own streams (the server), every release would
+   otherwise wait for the other requests' kernels.  A buffer is given back
+   only once the work using it has finished (its field's last run event, its
+   engine's stream).  When cudaMalloc fails, the kept blocks are freed and the
+   allocation is retried. */
+cudaError_t dmem_alloc(void** p, size_t bytes, size_t* got);
+void dmem_release(void* p, size_t bytes);
+
 /* grow-only device buffer: repeated runs of one configuration allocate once */
 template <typename T>
 struct DBuf
@@ -29,7 +40,7 @@ struct DBuf
 	~DBuf() { release(); }
 	void release()
 	{
-		if (ptr) cudaFree(ptr);
+		if (ptr) dmem_release(ptr, cap * sizeof(T));
 		ptr = nullptr;
 		cap = 0;
 		n = 0;
@@ -38,12 +49,14 @@ struct DBuf
 	{
 		n = count;
 		if (count <= cap && ptr) return cudaSuccess;
-		if (ptr) cudaFree(ptr);
+		if (ptr) cudaFree(ptr);   /* growing in a run: the stream may still use it */
 		ptr = nullptr;
 		cap = 0;
-		size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
-		cudaError_t e = cudaMalloc((void**)&ptr, bytes);
-		if (e == cudaSuccess) cap = std::max<size_t>(count, 1);
+		size_t bytes = std::max<size_t>(count, 1) * sizeof(T), got = 0;
+		cudaError_t e = dmem_alloc((void**)&ptr, bytes, &got);
+		if (e == cudaSuccess) cap = got / sizeof(T);
+		else ptr = nullptr;
+		n = count;
 		return e;
 	}
 	/* grow keeping the first `keep` elements */
@@ -51,13 +64,14 @@ struct DBuf
 	{
 		if (count <= cap && ptr) { n = count; return cudaSuccess; }
 		T* np = nullptr;
-		cudaError_t e = cudaMalloc((void**)&np, count * sizeof(T));
+		size_t got = 0;
+		cudaError_t e = dmem_alloc((void**)&np, count * sizeof(T), &got);
 		if (e != cudaSuccess) return e;
 		if (ptr && keep) cudaMemcpyAsync(np, ptr, keep * sizeof(T), cudaMemcpyDeviceToDevice, s);
 		cudaStreamSynchronize(s);
 		if (ptr) cudaFree(ptr);
 		ptr = np;
-		cap = count;
+		cap = got / sizeof(T);
 		n = count;
 		return cudaSuccess;
 	}
@@ -139,10 +153,11 @@ struct SolverPools
 	DBuf<unsigned char> fin_init, fin_cont;
 	DBuf<int> list_init, list_cont;
 	DBuf<double2> fval_init, fval_cont;   /* f, f' per root */
-	DBuf<RowDesc> rows_init, rows_cont, rows_rerun;
+	DBuf<RowDesc> rows_init, rows_cont, rows_rerun, rows_rerun2;
 	DBuf<unsigned long long> track_table;   /* column tables of the tracker */
-	DBuf<unsigned long long> row_stats;     /* TRACK_ROW_STATS per continuation row */
-	DBuf<int> rerun_count;                  /* [0] rows to re-run, [1] [2] tracker work counters */
+	DBuf<unsigned long long> row_stats, row_stats2;   /* TRACK_ROW_STATS per row: tracking, re-tracking */
+	DBuf<int> rerun_count;                  /* [0] rows to re-track, [1] [2] tracker work counters,
+	                                           [3] rows to re-run, [4] [5] re-tracking work counters */
 	DBuf<int> item_start;                   /* first tracker work item of each continuation row */
 	DBuf<int2> solo;                        /* tracker roots run alone, and their count after them */
 	DBuf<unsigned char> is_solo;            /* per continuation root */

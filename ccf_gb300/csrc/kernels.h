@@ -85,7 +85,8 @@ struct FieldOut
 	                                [4] unconverged, [5] max sweeps init, [6] max sweeps step,
 	                                [7] updates in the initial solve, [8] terms in the initial solve,
 	                                [9] continuation rows re-run by the full-sum solver, [10] tracker
-	                                sub-step halvings, [11] TRACK_* flags of the re-run rows */
+	                                sub-step halvings, [11] TRACK_* flags of the re-run rows,
+	                                [12] rows tracked again with fine sub-steps */
 };
 
 /* Outputs of step j of the continuation row (c, side).  Global step
@@ -158,6 +159,8 @@ struct SolveArgs
    bits), [1] TRACK_* flags, [2] most evaluations one root needed for one phi
    step, [3] points kept unconverged (the corrector stalled next to a zero). */
 constexpr int TRACK_ROW_STATS = 4;
+constexpr int TRACK_TSUB = 64;        /* a whole phi step in the tracker's sub-step units */
+constexpr int TRACK_FINE_SUB = 8;     /* longest sub-step when a failed row is tracked again */
 constexpr unsigned long long TRACK_DUPLICATE = 1;    /* two roots of a column on one zero */
 constexpr unsigned long long TRACK_LOST = 2;         /* a root that did not converge */
 constexpr unsigned long long TRACK_NONFINITE = 4;    /* a non-finite 1/mu bound */
@@ -178,6 +181,12 @@ struct TrackArgs
 	int2* solo;                 /* (row, root) of the roots that start off the root box: one warp each, first ... */
 	int* num_solo;              /* ... their number (zeroed before the marking launch) */
 	unsigned char* is_solo;     /* [master index]: the root runs solo, not in its item */
+	/* re-tracking of rows that failed the check: the rows are a device-side
+	   list of *num_rows_dev rows, items_per_row fixed-size items each (no
+	   solo roots), and a phi sub-step never longer than max_sub */
+	const int* num_rows_dev;    /* when set: the number of rows, on the device */
+	int items_per_row;          /* when > 0: item = row * items_per_row + chunk */
+	int max_sub;                /* longest sub-step (TSUB = a whole phi step) */
 };
 
 /* stars.cu */
@@ -219,6 +228,7 @@ cudaError_t launch_track_mark(cudaStream_t s, const TrackArgs& a);
 cudaError_t launch_phase_table(cudaStream_t s, int nb, int nphi, PhaseEntry* out);
 cudaError_t launch_track(cudaStream_t s, const TrackArgs& a, bool mixed);
 cudaError_t launch_collect_rerun(cudaStream_t s, const TrackArgs& a, RowDesc* rerun, int* count);
+cudaError_t launch_clear_tables(cudaStream_t s, const TrackArgs& a);
 cudaError_t launch_eval_points(cudaStream_t s, const FieldView* F_dev, int npts, const double2* z, const double* phi,
 	double2* f, double2* df, double2* w, double* err, double* mu);
 

@@ -712,7 +712,7 @@ dependence on the other roots.
     collect_rerun_kernel; re-run rows through the full-sum kernel. */
 
 constexpr int TNT = 128;                 /* threads per CTA of the tracker */
-constexpr int TSUB = 64;                 /* one phi step in sub-step units */
+constexpr int TSUB = TRACK_TSUB;         /* one phi step in sub-step units */
 constexpr int TRACK_ITERS = 6;           /* corrector iterations before the sub-step is halved */
 constexpr double TRACK_CONTRACT = 0.5;   /* each corrector step after the first must halve */
 constexpr double TRACK_CONTRACT_FINEST = 0.9;   /* ... or shrink by this at the finest sub-step */
@@ -1072,8 +1072,8 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 		int item = 0, solo_root = -1, row = 0;
 		if (lane == 0)
 		{
-			const int q = atomicAdd(&T.counter[0], 1);
-			if (q < *T.num_solo)
+			const int q = T.items_per_row > 0 ? 0 : atomicAdd(&T.counter[0], 1);
+			if (T.items_per_row == 0 && q < *T.num_solo)
 			{
 				const int2 sr = T.solo[q];
 				row = sr.x;
@@ -1086,7 +1086,12 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 		}
 		item = __shfl_sync(full, item, 0);
 		solo_root = __shfl_sync(full, solo_root, 0);
-		if (solo_root < 0)
+		if (T.items_per_row > 0)
+		{
+			if (item >= *T.num_rows_dev * T.items_per_row) break;
+			row = item / T.items_per_row;
+		}
+		else if (solo_root < 0)
 		{
 			if (item >= T.num_items) break;
 			row = item_row(T, item);
@@ -1107,8 +1112,10 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 		const RowDesc& RD = sR[w];
 		const TrackConst& K = sK[w];
 		const int R = F.num_roots;
-		const int a = solo_root >= 0 ? solo_root : (item - T.item_start[row]) * 32 + lane;
-		const bool valid = solo_root >= 0 ? lane == 0 : (a < R && !T.is_solo[RD.base + a]);
+		const int chunk = T.items_per_row > 0 ? item - row * T.items_per_row : item - T.item_start[row];
+		const int a = solo_root >= 0 ? solo_root : chunk * 32 + lane;
+		const bool valid = solo_root >= 0 ? lane == 0 : (a < R && (T.items_per_row > 0 || !T.is_solo[RD.base + a]));
+		const int max_sub = T.max_sub;
 		const int c = RD.branch, side = RD.side, nb = O.nb, nphi = O.nphi;
 		const int j0 = O.step_first, j1 = RD.steps;
 		const int cap = O.max_iters_step;
@@ -1131,7 +1138,7 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 
 		int j = j0;
 		bool act = valid;
-		int tt = j * TSUB;
+		int tt = min(t1 + max_sub, j * TSUB);
 		double2 z = z1;
 		double cp = 0, sp = 0;
 		dfl cpd = {0.f, 0.f}, spd = {0.f, 0.f};
@@ -1311,11 +1318,11 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 						evs = 0;
 						j++;
 						if (j > j1) act = false;
-						tn = j * TSUB;
+						tn = min(t1 + max_sub, j * TSUB);
 					}
 					else
 					{
-						tn = min(t1 + 2 * dist, j * TSUB);
+						tn = min(t1 + min(2 * dist, max_sub), j * TSUB);
 					}
 				}
 				else if (fail)
@@ -1384,13 +1391,15 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 	}
 }
 
-/* Rows the tracker flagged go to the re-run list (and count in stats[9]);
-   the others report their largest 1/mu bound, evaluations per step and
-   unconverged points. */
+/* Rows the tracker flagged go to the re-run list; the others report their
+   largest 1/mu bound, evaluations per step and unconverged points.  After
+   the first tracking the list is for the re-tracking (counted in
+   stats[12]); after the re-tracking, for the full-sum solver (stats[9],
+   their flags in stats[11]). */
 __global__ void collect_rerun_kernel(const TrackArgs T, RowDesc* rerun, int* count)
 {
 	const int r = blockIdx.x * blockDim.x + threadIdx.x;
-	if (r >= T.num_rows) return;
+	if (r >= (T.num_rows_dev ? *T.num_rows_dev : T.num_rows)) return;
 	const RowDesc row = T.rows[r];
 	const unsigned long long* rs = T.row_stats + TRACK_ROW_STATS * (size_t)r;
 	unsigned long long* st = T.outs[row.field].stats;
@@ -1398,8 +1407,15 @@ __global__ void collect_rerun_kernel(const TrackArgs T, RowDesc* rerun, int* cou
 	{
 		const int q = atomicAdd(count, 1);
 		rerun[q] = row;
-		atomicAdd(&st[9], 1ull);
-		atomicOr(&st[11], rs[1]);
+		if (T.items_per_row > 0)
+		{
+			atomicAdd(&st[9], 1ull);
+			atomicOr(&st[11], rs[1]);
+		}
+		else
+		{
+			atomicAdd(&st[12], 1ull);
+		}
 	}
 	else
 	{
@@ -1434,6 +1450,27 @@ cudaError_t launch_track(cudaStream_t s, const TrackArgs& a, bool mixed)
 	const int blocks = std::max(1, std::min(sms * n, (a.num_items + TNT / 32 - 1) / (TNT / 32)));
 	if (mixed) track_kernel<true><<<blocks, TNT, 0, s>>>(a);
 	else track_kernel<false><<<blocks, TNT, 0, s>>>(a);
+	return cudaGetLastError();
+}
+
+/* zeroes the column tables of the rows to re-track (a device-side list) */
+__global__ void clear_tables_kernel(const TrackArgs T)
+{
+	const int nrows = *T.num_rows_dev;
+	for (int q = blockIdx.y; q < nrows; q += gridDim.y)
+	{
+		const RowDesc row = T.rows[q];
+		const unsigned long long n = 2ull * T.fields[row.field].num_roots * row.steps;
+		unsigned long long* tab = T.table + row.cont_base;
+		for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+			i += (unsigned long long)gridDim.x * blockDim.x)
+			tab[i] = 0ull;
+	}
+}
+
+cudaError_t launch_clear_tables(cudaStream_t s, const TrackArgs& a)
+{
+	clear_tables_kernel<<<dim3(152, 16), 256, 0, s>>>(a);
 	return cudaGetLastError();
 }
 

@@ -165,7 +165,9 @@ typedef struct ccf_info
 	double near_mean;            /* mean number of stars in a leaf's near list */
 	int centres_solved;          /* branch centres solved by the initial Aberth solve (the
 	                                tracker solves every seg-th one and tracks the others) */
-	int reserved_int;
+	int rows_retracked;          /* tracker rows that failed the check and were tracked again
+	                                with sub-steps of 1/8 phi step (rows_rerun: those that
+	                                failed again and went to the full-sum solver) */
 } ccf_info;
 
 typedef struct ccf_handle ccf_handle;
