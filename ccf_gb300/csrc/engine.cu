@@ -473,6 +473,7 @@ ccf_status Engine::build_fmm(Field& f)
 
 	/* smooth-mass polynomials */
 	float4 inv_corner_df = make_float4(0, 0, 0, 0);
+	bool fold_ok = false;
 	SmoothPoly sp = smooth_polynomials(d.kappa_star, d.corner_x1, d.corner_x2, d.taylor_smooth);
 	{
 		std::vector<double2> d1(std::max(1, sp.m)), d2(std::max(1, sp.m)), a(sp.a.size());
@@ -516,6 +517,45 @@ ccf_status Engine::build_fmm(Field& f)
 		CCF_TRY(cudaMemcpyAsync(f.sm_d2.ptr, d2.data(), d2.size() * sizeof(double2), cudaMemcpyHostToDevice, s), "smooth");
 		CCF_TRY(cudaMemcpyAsync(f.sm_d2f.ptr, d2f.data(), d2f.size() * sizeof(float2), cudaMemcpyHostToDevice, s), "smooth");
 		CCF_TRY(cudaMemcpyAsync(f.sm_a.ptr, a.data(), a.size() * sizeof(double2), cudaMemcpyHostToDevice, s), "smooth");
+		/* the tracker's leaf blocks with the Taylor series folded in (rectangular
+		   Taylor smooth mass, mixed precision): the series conjugated into
+		   polynomials in z, built in long double */
+		fold_ok = p.precision == CCF_PRECISION_MIXED && d.rectangular && p.approx && sp.m > 0;
+		if (fold_ok)
+		{
+			typedef std::complex<long double> cl;
+			const cl icb = std::conj(cl((long double)sp.inv_corner.real(), (long double)sp.inv_corner.imag()));
+			const int M = sp.m, na = (int)sp.a.size();
+			std::vector<double2> coef(2 * M + 1 + 2 * M + na, make_double2(0, 0));
+			double2* ef = coef.data();
+			double2* er = ef + 2 * M + 1;
+			double2* eq = er + 2 * M;
+			cl pw(1.0L, 0.0L);
+			for (int m = 1; m <= M; m++)
+			{
+				pw *= icb * icb;   /* conj(1 / c)^(2m) */
+				const cl v1 = std::conj(cl(sp.d1[m - 1].real(), sp.d1[m - 1].imag())) * pw;
+				const cl v2 = std::conj(cl(sp.d2[m - 1].real(), sp.d2[m - 1].imag())) * pw;
+				ef[2 * m] = make_double2((double)v1.real(), (double)v1.imag());
+				er[2 * m - 1] = make_double2((double)v2.real(), (double)v2.imag());
+			}
+			const long double kpi = (long double)d.kappa_star / 3.14159265358979323846264338327950288L;
+			for (int n = 0; n < na; n++)
+			{
+				const cl v = cl(0.0L, kpi) * std::conj(cl(sp.a[n].real(), sp.a[n].imag()));
+				eq[n] = make_double2((double)v.real(), (double)v.imag());
+			}
+			CCF_TRY(f.fold_coef.ensure(coef.size()), "cudaMalloc(fold)");
+			CCF_TRY(cudaMemcpyAsync(f.fold_coef.ptr, coef.data(), coef.size() * sizeof(double2), cudaMemcpyHostToDevice, s),
+				"fold");
+			CCF_TRY(f.leaf_fold.ensure(nl), "cudaMalloc(fold)");
+			CCF_TRY(f.leaf_loc_df_fold.ensure((size_t)nl * 2 * (P + 1)), "cudaMalloc(fold)");
+			CCF_TRY(f.leaf_loc3f_fold.ensure((size_t)nl * (P + 1)), "cudaMalloc(fold)");
+			launch_fold_smooth(s, nl, P, f.leaf_center.ptr, f.leaf_inv_half.ptr, f.leaf_loc.ptr, f.fold_coef.ptr, 2 * M + 1,
+				f.fold_coef.ptr + 2 * M + 1, 2 * M, f.fold_coef.ptr + 4 * M + 1, na, 0.95 * std::hypot(d.corner_x1, d.corner_x2),
+				f.leaf_loc_df_fold.ptr, f.leaf_loc3f_fold.ptr, f.leaf_fold.ptr);
+			CCF_TRY(cudaGetLastError(), "fold_smooth_kernel");
+		}
 		CCF_TRY(cudaStreamSynchronize(s), "smooth");
 	}
 	int lerr = 0;
@@ -569,6 +609,9 @@ ccf_status Engine::build_fmm(Field& f)
 	V.inv_corner_df = inv_corner_df;
 	V.star_df = f.star_hilo.ptr;
 	V.star_mass_df = f.star_mass_df.ptr;
+	V.leaf_fold = fold_ok ? f.leaf_fold.ptr : nullptr;
+	V.leaf_loc_df_fold = fold_ok ? f.leaf_loc_df_fold.ptr : nullptr;
+	V.leaf_loc3f_fold = fold_ok ? f.leaf_loc3f_fold.ptr : nullptr;
 	CCF_TRY(f.view_dev.ensure(1), "cudaMalloc(view)");
 	CCF_TRY(cudaMemcpyAsync(f.view_dev.ptr, &V, sizeof(V), cudaMemcpyHostToDevice, s), "view");
 	return CCF_OK;
@@ -728,8 +771,12 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 				cost_c.push_back(cost * u.steps);
 			}
 		}
-		/* seeds of the solved centres of this field */
-		launch_seed_roots(s, N, R, K, f.star_gen.ptr, f.view.corner_abs, P.master_init.ptr + init_off[i],
+		/* seeds of the solved centres of this field, from the stars in tree
+		   order: consecutive roots (the lanes of a tracker warp) then start
+		   next to neighbouring stars, in the same or adjacent leaves, so their
+		   near-star loops and smooth-mass paths agree (the order of the roots
+		   within a column carries no meaning; a row stays one root's path) */
+		launch_seed_roots(s, N, R, K, f.star_pos.ptr, f.view.corner_abs, P.master_init.ptr + init_off[i],
 			mixed ? P.snap32_init.ptr + init_off[i] : nullptr, mixed ? nullptr : P.snap64_init.ptr + init_off[i]);
 	}
 	/* largest rows first */

@@ -116,8 +116,10 @@ struct Field
 	DBuf<NearStar> leaf_near;
 	DBuf<double2> leaf_loc;
 	DBuf<float2> leaf_loc3f;
-	DBuf<float4> leaf_near_df, leaf_loc_df;
-	DBuf<float2> leaf_mass_df, leaf_ih_df;
+	DBuf<float4> leaf_near_df, leaf_loc_df, leaf_loc_df_fold;
+	DBuf<float2> leaf_mass_df, leaf_ih_df, leaf_loc3f_fold;
+	DBuf<unsigned char> leaf_fold;
+	DBuf<double2> fold_coef;   /* the conjugated smooth-mass series in z, for the fold */
 	int num_leaves = 0;
 
 	/* smooth-mass polynomials */

@@ -87,6 +87,11 @@ struct FieldView
 	float4 inv_corner_df;
 	const float4* star_df;       /* [num_stars] star positions, split (x_hi, y_hi, x_lo, y_lo) */
 	const float2* star_mass_df;  /* [num_stars] */
+	/* the tracker's leaf blocks with the smooth-mass series folded in
+	   (fold_smooth_kernel); leaf_fold[leaf] = 1 where they hold */
+	const unsigned char* leaf_fold;
+	const float4* leaf_loc_df_fold;   /* like leaf_loc_df */
+	const float2* leaf_loc3f_fold;    /* like leaf_loc3f */
 };
 
 /* leaf containing z, or -1 when z lies outside the root box (the reference

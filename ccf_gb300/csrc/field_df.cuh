@@ -297,11 +297,13 @@ CCF_D TrackEval eval_track_df(const FieldView& F, const TrackConst& K, int leaf,
 	const float2 ihf = F.leaf_ih_df[leaf];
 	const dfl ih = {ihf.x, ihf.y};
 	const dfc dz = {df_mul(zr.re, ih), df_mul(zr.im, ih)};
-	const float4* L = F.leaf_loc_df + (size_t)leaf * 2 * (P + 1);
+	/* a leaf with the smooth-mass series folded into its expansion skips the series */
+	const bool folded = F.leaf_fold != nullptr && F.leaf_fold[leaf];
+	const float4* L = (folded ? F.leaf_loc_df_fold : F.leaf_loc_df) + (size_t)leaf * 2 * (P + 1);
 	const dfc al = horner_df(L, P, 1, dz);
 	const dfc dl = horner_df(L + (P + 1), P, 2, dz);
 	const float2 dzf = make_float2(dz.re.hi, dz.im.hi);
-	const float2* L3 = F.leaf_loc3f + (size_t)leaf * (P + 1);
+	const float2* L3 = (folded ? F.leaf_loc3f_fold : F.leaf_loc3f) + (size_t)leaf * (P + 1);
 	float2 d2l = L3[P];
 	for (int i = P - 1; i >= 3; i--) d2l = fadd(fmulc(d2l, dzf), L3[i]);
 
@@ -312,8 +314,14 @@ CCF_D TrackEval eval_track_df(const FieldView& F, const TrackConst& K, int leaf,
 	float2 d2s;
 	const float zx = (float)z.x, zy = (float)z.y;
 	const bool taylor = F.rectangular && F.approx && F.smooth_m > 0 && zx * zx + zy * zy < K.r2;
-	e.wmode = taylor ? 1 : 0;
-	if (taylor)
+	e.wmode = (taylor || folded) ? 1 : 0;
+	if (folded)
+	{
+		/* the series are in the leaf's blocks: only d alpha_s / d zbar's constant */
+		ds = {K.k1, {0.f, 0.f}};
+		d2s = make_float2(0.f, 0.f);
+	}
+	else if (taylor)
 	{
 		const dfc zb = dfc_from(make_double2(z.x, -z.y));
 		const dfc wc = dfc_mul(zb, dfc_load(F.inv_corner_df));   /* zbar / c */

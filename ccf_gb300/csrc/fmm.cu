@@ -329,3 +329,88 @@ void launch_leaf_df(cudaStream_t s, int num_leaves, int P, const double2* leaf_c
 }
 
 } /* namespace ccf */
+
+namespace ccf
+{
+
+/* The smooth-mass Taylor series of the rectangular field, folded into the
+   local expansion of every leaf where that is exact to the evaluation's
+   rounding, for the continuation tracker.  The three series enter the
+   evaluators conjugated, as polynomials in z: conj(d alpha_s / d zbar) - k1
+   with f's local alpha'' block (ef), conj(d2 alpha_s / d zbar2) with f''s
+   alpha''' block (er), and conj of the anti-analytic part of alpha_s with the
+   lens map's alpha block (eq).  Shifted to the leaf centre and scaled to the
+   leaf's dz = (z - centre) / h, a polynomial adds to the block's
+   coefficients up to the expansion order; the leaf is folded when the terms
+   beyond it sum to less than 1e-15 at |dz| = sqrt 2 (the corner of the leaf)
+   and the leaf lies inside 0.95 of the corner circle, where the series
+   converges.  One thread per leaf; the FP64 blocks stay as they are (the
+   direct evaluators keep using them with the series). */
+constexpr int FOLD_MAXD = 256;
+
+CCF_D double fold_shift(const double2* e, int n, double2 z0, double h, int keep, double2* b)
+{
+	double2 t[FOLD_MAXD];
+	for (int i = 0; i < n; i++) t[i] = e[i];
+	/* repeated synthetic division: t[j] = sum_{k >= j} C(k, j) e_k z0^(k - j) */
+	for (int i = 0; i + 1 < n; i++)
+		for (int k = n - 2; k >= i; k--) t[k] = cadd(t[k], cmul(z0, t[k + 1]));
+	double hj = 1, tail = 0, r = 1;
+	for (int j = 0; j < n; j++)
+	{
+		const double2 v = make_double2(t[j].x * hj, t[j].y * hj);
+		if (j < keep) b[j] = v;
+		else tail += hypot(v.x, v.y) * r;
+		hj *= h;
+		r *= 1.4142135623730951;
+	}
+	for (int j = n; j < keep; j++) b[j] = make_double2(0, 0);
+	return tail;
+}
+
+__global__ void fold_smooth_kernel(int num_leaves, int P, const double2* __restrict__ leaf_center,
+	const double* __restrict__ leaf_inv_half, const double2* __restrict__ loc, const double2* __restrict__ ef, int nf,
+	const double2* __restrict__ er, int nr, const double2* __restrict__ eq, int nq, double radius,
+	float4* __restrict__ loc_df, float2* __restrict__ loc3f, unsigned char* __restrict__ fold)
+{
+	const int l = blockIdx.x * blockDim.x + threadIdx.x;
+	if (l >= num_leaves) return;
+	const double2 c = leaf_center[l];
+	const double h = 1.0 / leaf_inv_half[l];
+	fold[l] = 0;
+	if (hypot(c.x, c.y) + 1.4142135623730951 * h > radius || nf > FOLD_MAXD || nr > FOLD_MAXD || nq > FOLD_MAXD) return;
+	double2 p[FOLD_MAXD], r[FOLD_MAXD], q[FOLD_MAXD];
+	const double tol = 1e-15;
+	if (fold_shift(ef, nf, c, h, P - 1, p) > tol) return;   /* block 1 holds dz^0 .. dz^(P-2) */
+	if (fold_shift(er, nr, c, h, P - 2, r) > tol) return;   /* block 2 holds dz^0 .. dz^(P-3) */
+	if (fold_shift(eq, nq, c, h, P, q) > tol) return;       /* block 0 holds dz^0 .. dz^(P-1) */
+	auto split = [](double x) {
+		float hi = __double2float_rn(x);
+		return make_float2(hi, __double2float_rn(x - (double)hi));
+	};
+	for (int i = 0; i <= P; i++)
+	{
+		double2 a0 = loc[((size_t)l * 3 + 0) * (P + 1) + i];
+		double2 a1 = loc[((size_t)l * 3 + 1) * (P + 1) + i];
+		double2 a2 = loc[((size_t)l * 3 + 2) * (P + 1) + i];
+		if (i >= 1) a0 = cadd(a0, q[i - 1]);
+		if (i >= 2) a1 = cadd(a1, p[i - 2]);
+		if (i >= 3) a2 = cadd(a2, r[i - 3]);
+		const float2 x0 = split(a0.x), y0 = split(a0.y), x1 = split(a1.x), y1 = split(a1.y);
+		loc_df[((size_t)l * 2 + 0) * (P + 1) + i] = make_float4(x0.x, y0.x, x0.y, y0.y);
+		loc_df[((size_t)l * 2 + 1) * (P + 1) + i] = make_float4(x1.x, y1.x, x1.y, y1.y);
+		loc3f[(size_t)l * (P + 1) + i] = make_float2((float)a2.x, (float)a2.y);
+	}
+	fold[l] = 1;
+}
+
+void launch_fold_smooth(cudaStream_t s, int num_leaves, int P, const double2* leaf_center, const double* leaf_inv_half,
+	const double2* loc, const double2* ef, int nf, const double2* er, int nr, const double2* eq, int nq, double radius,
+	float4* loc_df, float2* loc3f, unsigned char* fold)
+{
+	if (num_leaves <= 0) return;
+	fold_smooth_kernel<<<(num_leaves + 63) / 64, 64, 0, s>>>(num_leaves, P, leaf_center, leaf_inv_half, loc, ef, nf, er,
+		nr, eq, nq, radius, loc_df, loc3f, fold);
+}
+
+} /* namespace ccf */

@@ -220,6 +220,9 @@ void launch_leaf_build(cudaStream_t s, const TreeDev& T, int num_nodes, const in
 void launch_leaf_df(cudaStream_t s, int num_leaves, int P, const double2* leaf_center, const double* leaf_inv_half,
 	const int* near_count, const NearStar* near, const double2* loc, float4* near_df, float2* mass_df, float4* loc_df,
 	float2* ih_df);
+void launch_fold_smooth(cudaStream_t s, int num_leaves, int P, const double2* leaf_center, const double* leaf_inv_half,
+	const double2* loc, const double2* ef, int nf, const double2* er, int nr, const double2* eq, int nq, double radius,
+	float4* loc_df, float2* loc3f, unsigned char* fold);
 
 /* solver.cu */
 int solver_blocks_per_sm(bool mixed);
