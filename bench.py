@@ -408,8 +408,10 @@ def run_multi(args) -> None:
             pts = reduce(float(r["points"]), SUM)
             lat = r["latency"]
             # the plain-FP64 comparison replays the first requests of at most
-            # 5000 stars (a 50000-star field takes minutes in plain FP64)
-            sub = [q for q in reqs if q[1]["num_stars"] <= 5000][:args.fp64_requests]
+            # 5000 stars (a 50000-star field takes minutes in plain FP64), all
+            # submitted at once in both precisions: a throughput comparison, not
+            # bounded by the arrival times of the stream
+            sub = [(0.0, q[1]) for q in reqs if q[1]["num_stars"] <= 5000][:args.fp64_requests]
             r64 = stream("fp64", sub) if sub else None
             rm = stream("mixed", sub) if sub else None
             line.update({"value": pts / span, "ms_per_step": 1e3 * span, "steps": 1, "scaling": "weak",
@@ -424,7 +426,8 @@ def run_multi(args) -> None:
                          "e2e": {"value": pts / span, "unit": "points/s", "h2d_bytes_per_step": 0,
                                  "d2h_bytes_per_step": 0},
                          "server": dict(r["stats"]),
-                         "fp64_plain": {"requests": len(sub), "value": r64["points"] / r64["span"],
+                         "fp64_plain": {"requests": len(sub), "arrivals": "all at once",
+                                        "value": r64["points"] / r64["span"],
                                         "mixed_same_requests": rm["points"] / rm["span"], "unit": "points/s",
                                         "ratio_mixed_over_fp64": (rm["points"] / rm["span"]) / (r64["points"] / r64["span"])}
                          if sub else None,

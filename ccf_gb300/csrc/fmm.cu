@@ -344,28 +344,46 @@ namespace ccf
    coefficients up to the expansion order; the leaf is folded when the terms
    beyond it sum to less than 1e-15 at |dz| = sqrt 2 (the corner of the leaf)
    and the leaf lies inside 0.95 of the corner circle, where the series
-   converges.  One thread per leaf; the FP64 blocks stay as they are (the
-   direct evaluators keep using them with the series). */
+   converges.  One warp per leaf, lane i building coefficient i of the three
+   blocks (the expansion order is at most 31); the FP64 blocks stay as they
+   are (the direct evaluators keep using them with the series). */
 constexpr int FOLD_MAXD = 256;
+static_assert(MAX_ORDER < 32, "one coefficient of a leaf block per lane");
 
-CCF_D double fold_shift(const double2* e, int n, double2 z0, double h, int keep, double2* b)
+/* h^j times the j-th Taylor coefficient at z0 of sum_k e_k z^k, i.e.
+   h^j sum_{k >= j} C(k, j) e_k z0^(k - j): Horner from the top degree with
+   the binomial carried down the column, C(k, j) = C(k + 1, j) (k + 1 - j) / (k + 1)
+   (inv[k] = 1 / k).  Zero for j outside [0, n). */
+CCF_D double2 fold_coef(const double2* __restrict__ e, int n, double2 z0, double h, int j, const double* inv)
 {
-	double2 t[FOLD_MAXD];
-	for (int i = 0; i < n; i++) t[i] = e[i];
-	/* repeated synthetic division: t[j] = sum_{k >= j} C(k, j) e_k z0^(k - j) */
-	for (int i = 0; i + 1 < n; i++)
-		for (int k = n - 2; k >= i; k--) t[k] = cadd(t[k], cmul(z0, t[k + 1]));
-	double hj = 1, tail = 0, r = 1;
-	for (int j = 0; j < n; j++)
+	if (j < 0 || j >= n) return make_double2(0, 0);
+	double b = 1;   /* C(n - 1, j) */
+	for (int i = 0; i < j; i++) b *= (double)(n - 1 - i) * inv[i + 1];
+	double2 acc = make_double2(b * e[n - 1].x, b * e[n - 1].y);
+	for (int k = n - 2; k >= j; k--)
 	{
-		const double2 v = make_double2(t[j].x * hj, t[j].y * hj);
-		if (j < keep) b[j] = v;
-		else tail += hypot(v.x, v.y) * r;
-		hj *= h;
-		r *= 1.4142135623730951;
+		b *= (double)(k + 1 - j) * inv[k + 1];
+		const double2 ek = e[k];
+		acc = cmul(acc, z0);
+		acc.x += b * ek.x;
+		acc.y += b * ek.y;
 	}
-	for (int j = n; j < keep; j++) b[j] = make_double2(0, 0);
-	return tail;
+	double hj = 1;
+	for (int i = 0; i < j; i++) hj *= h;
+	return make_double2(acc.x * hj, acc.y * hj);
+}
+
+/* sum over j = start, start + 32, ... < n of |coefficient j| sqrt(2)^j: one
+   lane's share of the terms beyond a block's order at the leaf corner */
+CCF_D double fold_tail(const double2* __restrict__ e, int n, double2 z0, double h, int start, const double* inv)
+{
+	double t = 0;
+	for (int j = start; j < n; j += 32)
+	{
+		const double2 v = fold_coef(e, n, z0, h, j, inv);
+		t += hypot(v.x, v.y) * ldexp((j & 1) ? 1.4142135623730951 : 1.0, j >> 1);
+	}
+	return t;
 }
 
 __global__ void fold_smooth_kernel(int num_leaves, int P, const double2* __restrict__ leaf_center,
@@ -373,35 +391,50 @@ __global__ void fold_smooth_kernel(int num_leaves, int P, const double2* __restr
 	const double2* __restrict__ er, int nr, const double2* __restrict__ eq, int nq, double radius,
 	float4* __restrict__ loc_df, float2* __restrict__ loc3f, unsigned char* __restrict__ fold)
 {
-	const int l = blockIdx.x * blockDim.x + threadIdx.x;
+	__shared__ double inv[FOLD_MAXD + 1];
+	for (int k = threadIdx.x; k <= FOLD_MAXD; k += blockDim.x) inv[k] = k ? 1.0 / k : 0.0;
+	__syncthreads();
+	const int lane = threadIdx.x & 31;
+	const int l = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
 	if (l >= num_leaves) return;
 	const double2 c = leaf_center[l];
 	const double h = 1.0 / leaf_inv_half[l];
-	fold[l] = 0;
-	if (hypot(c.x, c.y) + 1.4142135623730951 * h > radius || nf > FOLD_MAXD || nr > FOLD_MAXD || nq > FOLD_MAXD) return;
-	double2 p[FOLD_MAXD], r[FOLD_MAXD], q[FOLD_MAXD];
+	if (hypot(c.x, c.y) + 1.4142135623730951 * h > radius || nf > FOLD_MAXD || nr > FOLD_MAXD || nq > FOLD_MAXD)
+	{
+		if (lane == 0) fold[l] = 0;
+		return;
+	}
+	/* block 0 (alpha) gains dz^0 .. dz^(P-1) of eq at its coefficients 1 .. P,
+	   block 1 (f's alpha'' block) dz^0 .. dz^(P-2) of ef at 2 .. P, block 2
+	   (f''s alpha''' block) dz^0 .. dz^(P-3) of er at 3 .. P */
+	const int i = lane;
+	const double2 q = i >= 1 && i <= P ? fold_coef(eq, nq, c, h, i - 1, inv) : make_double2(0, 0);
+	const double2 pf = i >= 2 && i <= P ? fold_coef(ef, nf, c, h, i - 2, inv) : make_double2(0, 0);
+	const double2 r = i >= 3 && i <= P ? fold_coef(er, nr, c, h, i - 3, inv) : make_double2(0, 0);
+	double tq = fold_tail(eq, nq, c, h, P + lane, inv);
+	double tp = fold_tail(ef, nf, c, h, P - 1 + lane, inv);
+	double tr = fold_tail(er, nr, c, h, P - 2 + lane, inv);
+	for (int o = 16; o; o >>= 1)
+	{
+		tq += __shfl_xor_sync(0xffffffffu, tq, o);
+		tp += __shfl_xor_sync(0xffffffffu, tp, o);
+		tr += __shfl_xor_sync(0xffffffffu, tr, o);
+	}
 	const double tol = 1e-15;
-	if (fold_shift(ef, nf, c, h, P - 1, p) > tol) return;   /* block 1 holds dz^0 .. dz^(P-2) */
-	if (fold_shift(er, nr, c, h, P - 2, r) > tol) return;   /* block 2 holds dz^0 .. dz^(P-3) */
-	if (fold_shift(eq, nq, c, h, P, q) > tol) return;       /* block 0 holds dz^0 .. dz^(P-1) */
+	const bool ok = tq <= tol && tp <= tol && tr <= tol;
+	if (lane == 0) fold[l] = ok ? 1 : 0;
+	if (!ok || i > P) return;
 	auto split = [](double x) {
 		float hi = __double2float_rn(x);
 		return make_float2(hi, __double2float_rn(x - (double)hi));
 	};
-	for (int i = 0; i <= P; i++)
-	{
-		double2 a0 = loc[((size_t)l * 3 + 0) * (P + 1) + i];
-		double2 a1 = loc[((size_t)l * 3 + 1) * (P + 1) + i];
-		double2 a2 = loc[((size_t)l * 3 + 2) * (P + 1) + i];
-		if (i >= 1) a0 = cadd(a0, q[i - 1]);
-		if (i >= 2) a1 = cadd(a1, p[i - 2]);
-		if (i >= 3) a2 = cadd(a2, r[i - 3]);
-		const float2 x0 = split(a0.x), y0 = split(a0.y), x1 = split(a1.x), y1 = split(a1.y);
-		loc_df[((size_t)l * 2 + 0) * (P + 1) + i] = make_float4(x0.x, y0.x, x0.y, y0.y);
-		loc_df[((size_t)l * 2 + 1) * (P + 1) + i] = make_float4(x1.x, y1.x, x1.y, y1.y);
-		loc3f[(size_t)l * (P + 1) + i] = make_float2((float)a2.x, (float)a2.y);
-	}
-	fold[l] = 1;
+	const double2 a0 = cadd(loc[((size_t)l * 3 + 0) * (P + 1) + i], q);
+	const double2 a1 = cadd(loc[((size_t)l * 3 + 1) * (P + 1) + i], pf);
+	const double2 a2 = cadd(loc[((size_t)l * 3 + 2) * (P + 1) + i], r);
+	const float2 x0 = split(a0.x), y0 = split(a0.y), x1 = split(a1.x), y1 = split(a1.y);
+	loc_df[((size_t)l * 2 + 0) * (P + 1) + i] = make_float4(x0.x, y0.x, x0.y, y0.y);
+	loc_df[((size_t)l * 2 + 1) * (P + 1) + i] = make_float4(x1.x, y1.x, x1.y, y1.y);
+	loc3f[(size_t)l * (P + 1) + i] = make_float2((float)a2.x, (float)a2.y);
 }
 
 void launch_fold_smooth(cudaStream_t s, int num_leaves, int P, const double2* leaf_center, const double* leaf_inv_half,
@@ -409,7 +442,8 @@ void launch_fold_smooth(cudaStream_t s, int num_leaves, int P, const double2* le
 	float4* loc_df, float2* loc3f, unsigned char* fold)
 {
 	if (num_leaves <= 0) return;
-	fold_smooth_kernel<<<(num_leaves + 63) / 64, 64, 0, s>>>(num_leaves, P, leaf_center, leaf_inv_half, loc, ef, nf, er,
+	const int warps = 4;
+	fold_smooth_kernel<<<(num_leaves + warps - 1) / warps, warps * 32, 0, s>>>(num_leaves, P, leaf_center, leaf_inv_half, loc, ef, nf, er,
 		nr, eq, nq, radius, loc_df, loc3f, fold);
 }
 
