@@ -377,11 +377,14 @@ CCF_D TrackEval eval_track_df(const FieldView& F, const TrackConst& K, int leaf,
 	e.as2 = st.x * st.x + st.y * st.y;
 	/* |f| at z - st: f - f' st (f holomorphic), the FP32 error of f' st, the
 	   double-float rounding of the terms of f (2^-47 of their sizes) and half
-	   the FP64 spacing of the root times |f'| */
+	   the FP64 spacing of the root times |f'|.  The difference is formed in
+	   FP64 and its modulus taken in FP32, rounded up by 2^-20 (the FP32
+	   roundings of the sum are a few 2^-24): a bound, not an estimate */
 	const float2 fsv = fmulc(df, st);
 	const float terms = t2 * tabs + hypotf(dl.re.hi, dl.im.hi) + hypotf(ds.re.hi, ds.im.hi) + fabsf(a.hi) + fabsf(K.shear.hi);
-	e.af = hypot(e.fz.x - (double)fsv.x, e.fz.y - (double)fsv.y) +
-		(double)(1e-6f * hypotf(fsv.x, fsv.y) + 7.2e-15f * terms + 1.2e-16f * hypotf(zx, zy) * hypotf(df.x, df.y));
+	const float res = hypotf((float)(e.fz.x - (double)fsv.x), (float)(e.fz.y - (double)fsv.y));
+	e.af = (double)((res + 1e-6f * hypotf(fsv.x, fsv.y) + 7.2e-15f * terms + 1.2e-16f * hypotf(zx, zy) * hypotf(df.x, df.y)) *
+		(1.f + 0x1p-20f));
 	/* w - the linear terms: (-theta^2 s1.x - al.x - sa.x, theta^2 s1.y + al.y - sa.y) (eval_point_df) */
 	dfl wr = df_neg(df_mul(K.theta2, s1.re));
 	wr = df_add(wr, df_neg(al.re));

@@ -38,6 +38,7 @@ GB300 design:
 #include "kernels.h"
 
 #include <cooperative_groups.h>
+#include <type_traits>
 
 namespace cg = cooperative_groups;
 
@@ -1120,7 +1121,11 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 		const int j0 = O.step_first, j1 = RD.steps;
 		const int cap = O.max_iters_step;
 		const double tol = STEP_TOL * F.theta;
-		const double tol2 = tol * tol;
+		/* the corrector's decisions compare squared step sizes, in FP32 when
+		   the step itself is FP32 */
+		typedef typename std::conditional<MIXED, float, double>::type real;
+		const real tol2 = (real)(tol * tol);
+		const real stuck2 = (real)(TRACK_STUCK * TRACK_STUCK * F.theta * F.theta);
 		const bool disc_exact = !F.rectangular && !F.approx;
 		const double inv_cell = CELL_PER_THETA / F.theta;
 		const unsigned long long slots = 2ull * (unsigned long long)R;
@@ -1144,7 +1149,7 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 		dfl cpd = {0.f, 0.f}, spd = {0.f, 0.f};
 		track_phase(O, c, side, tt, cp, sp, cpd, spd);
 		int it = 0, evs = 0;
-		double prev2 = 0;
+		real prev2 = 0;
 		bool lost = !valid;
 		bool refine = false;
 		unsigned unconv = 0;
@@ -1163,7 +1168,7 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 			}
 			const bool off = act && leaf < 0;
 			double2 step = make_double2(0, 0);
-			double as2 = 0;
+			real as2 = 0;
 			TrackEval e;
 			e.step = make_float2(0.f, 0.f);
 			e.as2 = 0;
@@ -1180,7 +1185,7 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 					if (off) e = o;
 				}
 				step = make_double2((double)e.step.x, (double)e.step.y);
-				as2 = (double)e.as2;
+				as2 = e.as2;
 			}
 			else
 			{
@@ -1212,7 +1217,7 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 				/* at the finest sub-step the corrector may take linear steps (a
 				   pair of close zeros) as long as they keep shrinking */
 				const bool finest = tt - t1 <= 1;
-				const double contract = finest ? TRACK_CONTRACT_FINEST : TRACK_CONTRACT;
+				const real contract = (real)(finest ? TRACK_CONTRACT_FINEST : TRACK_CONTRACT);
 				bool conv = false, fail = !isfinite(as2);
 				if (!fail && it > 0 && as2 >= tol2 && as2 > contract * contract * prev2) fail = true;
 				if (!fail)
@@ -1234,7 +1239,7 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 					else if (it >= (finest ? iters_finest : iters)) fail = true;
 				}
 				if (!fail) z = csub(z, step);
-				if (fail && finest && isfinite(as2) && as2 < TRACK_STUCK * TRACK_STUCK * F.theta * F.theta)
+				if (fail && finest && isfinite(as2) && as2 < stuck2)
 				{
 					/* the corrector stalls next to a zero (nearly coincident zeros,
 					   or neighbouring leaf expansions meeting with a small jump in
