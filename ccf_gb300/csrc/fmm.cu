@@ -25,44 +25,67 @@ CCF_D double binom_at(const double* __restrict__ B, int n, int k)
 	return B[n * (n + 1) / 2 + k];
 }
 
-CCF_D double2 cpow_int(double2 a, int p)
+/* t^lane on every lane of the warp (t^0 = 1): a product scan, five complex
+   products instead of lane-many.  All 32 lanes must call it. */
+CCF_D double2 warp_powers(double2 t, int lane)
 {
-	double2 r = make_double2(1, 0);
-	for (int i = 0; i < p; i++) r = cmul(r, a);
-	return r;
+	double2 x = lane == 0 ? make_double2(1, 0) : t;
+	for (int o = 1; o < 32; o <<= 1)
+	{
+		const double2 y = make_double2(__shfl_up_sync(0xffffffffu, x.x, o), __shfl_up_sync(0xffffffffu, x.y, o));
+		if (lane >= o) x = cmul(y, x);
+	}
+	return x;
 }
 
-/* upward pass at one level: P2M for leaves holding stars, M2M for split nodes */
+CCF_D double2 shfl_c(double2 v, int src)
+{
+	return make_double2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+
+/* upward pass at one level: P2M for leaves holding stars, M2M for split
+   nodes.  The stars of a leaf are taken 32 at a time, one per lane, and
+   handed round the warp by shuffles; the powers come from warp_powers. */
 __global__ void fmm_upward_kernel(TreeDev T, int start, int count, int P, const double2* __restrict__ pos,
 	const double* __restrict__ mass, double2* __restrict__ multi, const double* __restrict__ B)
 {
 	int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	int p = threadIdx.x & 31;
-	if (w >= count) return;
+	if (w >= count) return;   /* warp-uniform */
 	int n = start + w;
-	if (p > P) return;
+	const bool act = p <= P;
 	double2 r = make_double2(0, 0);
 	int ch = T.child[n];
 	if (ch < 0)
 	{
 		int s = T.star_start[n], ns = T.star_count[n];
-		if (ns == 0) return;
+		if (ns == 0) return;   /* warp-uniform */
 		double2 c = T.center[n];
 		double ih = 1.0 / T.half[n];
-		for (int i = 0; i < ns; i++)
+		for (int i0 = 0; i0 < ns; i0 += 32)
 		{
-			double m = mass[s + i];
-			if (p == 0)
+			const int nq = min(32, ns - i0);
+			double mq = 0;
+			double2 wq = make_double2(0, 0);
+			if (p < nq)
 			{
-				r.x += m;
+				const double2 q = pos[s + i0 + p];
+				mq = mass[s + i0 + p];
+				wq = make_double2((q.x - c.x) * ih, (q.y - c.y) * ih);
 			}
-			else
+			for (int i = 0; i < nq; i++)
 			{
-				double2 q = pos[s + i];
-				double2 wz = make_double2((q.x - c.x) * ih, (q.y - c.y) * ih);
-				double2 t = cpow_int(wz, p);
-				r.x -= t.x * m;
-				r.y -= t.y * m;
+				const double m = __shfl_sync(0xffffffffu, mq, i);
+				const double2 t = warp_powers(shfl_c(wq, i), p);
+				if (p == 0)
+				{
+					r.x += m;
+				}
+				else
+				{
+					r.x -= t.x * m;
+					r.y -= t.y * m;
+				}
 			}
 		}
 		if (p > 0)
@@ -78,44 +101,51 @@ __global__ void fmm_upward_kernel(TreeDev T, int start, int count, int P, const 
 		{
 			int k = ch + q;
 			const double2* a = multi + (size_t)k * (P + 1);
-			double2 v;
+			double2 cc = T.center[k];
+			double ih = 1.0 / T.half[k];
+			double2 dz = make_double2((cc.x - pc.x) * ih, (cc.y - pc.y) * ih);
+			const double2 dzp = warp_powers(dz, p);
+			double2 v = make_double2(0, 0);
 			if (p == 0)
 			{
 				v = a[0];
 			}
-			else
+			else if (act)
 			{
-				double2 cc = T.center[k];
-				double ih = 1.0 / T.half[k];
-				double2 dz = make_double2((cc.x - pc.x) * ih, (cc.y - pc.y) * ih);
 				/* b_p = (sum_{i=1..p} a_i C(p-1, i-1) dz^(p-i) - a_0 dz^p / p) / 2^p */
 				double2 acc = cscale(a[1], binom_at(B, p - 1, 0));
 				for (int i = 2; i <= p; i++) acc = cadd(cmul(acc, dz), cscale(a[i], binom_at(B, p - 1, i - 1)));
-				double2 dzp = cpow_int(dz, p);
 				double2 t = cscale(cmul(a[0], dzp), 1.0 / p);
 				v = cscale(csub(acc, t), ldexp(1.0, -p));
 			}
 			r = cadd(r, v);
 		}
 	}
-	multi[(size_t)n * (P + 1) + p] = r;
+	if (act) multi[(size_t)n * (P + 1) + p] = r;
 }
 
 /* downward pass at one level >= 2: L2L from the parent, then M2L from the
    same-level interaction list, then P2L from the coarser-leaf list, summed
-   in that order (include/ccf.cuh:880-893) */
+   in that order (include/ccf.cuh:880-893).  GB300's FP64 pipe is 1/64 of its
+   FP32 one, so the translations are arranged for few FP64 operations per
+   lane: the per-source constants (the M2L ratio t = -1/dz and log(-dz); the
+   P2L star offsets and their logs) are formed once, one source per lane, and
+   handed round by shuffles; lane p takes t^p from a product scan; and the
+   M2L sum over k is a binomial-weighted sum of the pre-scaled b_k t^k (two
+   FMAs a term) instead of a complex Horner recurrence. */
 __global__ void fmm_downward_kernel(TreeDev T, int start, int count, int P, const double2* __restrict__ pos,
 	const double* __restrict__ mass, const double2* __restrict__ multi, double2* __restrict__ local,
 	const double* __restrict__ B)
 {
 	int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	int p = threadIdx.x & 31;
-	if (w >= count) return;
+	if (w >= count) return;   /* warp-uniform */
 	int n = start + w;
-	if (p > P) return;
+	const bool act = p <= P;
 	double2 cn = T.center[n];
 	double2 r = make_double2(0, 0);
 	/* L2L: d_p = sum_{k>=max(p,1)} c_k C(k,p) dz^(k-p) / 2^p, dz = (c - c_parent)/h_parent */
+	if (act)
 	{
 		int par = T.parent[n];
 		const double2* cl = local + (size_t)par * (P + 1);
@@ -131,29 +161,47 @@ __global__ void fmm_downward_kernel(TreeDev T, int start, int count, int P, cons
 	/* M2L: t = 1/(-dz), dz = (c_from - c_to)/h_from;
 	   c_0 = sum_k b_k t^k + b_0 log(-dz) + b_0 log h_from
 	   c_p = (sum_k b_k C(p+k-1, k-1) t^k - b_0/p) (-t)^p */
-	int nm = T.m2l_count[n];
+	const int nm = T.m2l_count[n];
+	static_assert(MAX_M2L <= 32, "one interaction per lane");
+	int fq = 0;
+	double2 tq = make_double2(0, 0), lq = make_double2(0, 0);
+	double hq = 0;
+	if (p < nm)
+	{
+		fq = T.m2l[n * MAX_M2L + p];
+		const double2 cf = T.center[fq];
+		const double hf = T.half[fq];
+		const double ih = 1.0 / hf;
+		const double2 dz = make_double2((cf.x - cn.x) * ih, (cf.y - cn.y) * ih);
+		tq = cinv(make_double2(-dz.x, -dz.y));
+		lq = make_double2(log(hypot(dz.x, dz.y)), atan2(-dz.y, -dz.x));
+		hq = log(hf);
+	}
 	for (int j = 0; j < nm; j++)
 	{
-		int f = T.m2l[n * MAX_M2L + j];
+		const int f = __shfl_sync(0xffffffffu, fq, j);
+		const double2 t = shfl_c(tq, j);
+		const double2 lg = shfl_c(lq, j);
+		const double lh = __shfl_sync(0xffffffffu, hq, j);
 		const double2* b = multi + (size_t)f * (P + 1);
-		double2 cf = T.center[f];
-		double hf = T.half[f];
-		double ih = 1.0 / hf;
-		double2 dz = make_double2((cf.x - cn.x) * ih, (cf.y - cn.y) * ih);
-		double2 t = cinv(make_double2(-dz.x, -dz.y));
-		double2 acc = cscale(b[P], binom_at(B, p + P - 1, P - 1));
-		for (int k = P - 1; k >= 1; k--) acc = cadd(cmul(acc, t), cscale(b[k], binom_at(B, p + k - 1, k - 1)));
-		acc = cmul(acc, t);
+		const double2 tp = warp_powers(t, p);
+		const double2 bt = act && p >= 1 ? cmul(b[p], tp) : make_double2(0, 0);   /* b_p t^p on lane p */
+		double2 acc = make_double2(0, 0);
+		for (int k = P; k >= 1; k--)
+		{
+			const double2 v = shfl_c(bt, k);
+			if (act) acc = cadd(acc, cscale(v, binom_at(B, p + k - 1, k - 1)));
+		}
+		if (!act) continue;
 		double2 v;
 		if (p == 0)
 		{
-			double2 lg = make_double2(log(hypot(dz.x, dz.y)), atan2(-dz.y, -dz.x));
-			v = cadd(cadd(acc, cmul(b[0], lg)), cscale(b[0], log(hf)));
+			v = cadd(cadd(acc, cmul(b[0], lg)), cscale(b[0], lh));
 		}
 		else
 		{
-			double2 mt = make_double2(-t.x, -t.y);
-			v = cmul(csub(acc, cscale(b[0], 1.0 / p)), cpow_int(mt, p));
+			const double2 mtp = (p & 1) ? make_double2(-tp.x, -tp.y) : tp;   /* (-t)^p */
+			v = cmul(csub(acc, cscale(b[0], 1.0 / p)), mtp);
 		}
 		r = cadd(r, v);
 	}
@@ -162,33 +210,45 @@ __global__ void fmm_downward_kernel(TreeDev T, int start, int count, int P, cons
 	double hn = T.half[n];
 	double ihn = 1.0 / hn;
 	double lhn = log(hn);
+	const double ip = p > 0 ? 1.0 / p : 0.0;
 	for (int j = 0; j < np; j++)
 	{
 		int f = T.p2l[n * MAX_P2L + j];
 		int s = T.star_start[f], ns = T.star_count[f];
 		double2 v = make_double2(0, 0);
-		for (int i = 0; i < ns; i++)
+		for (int i0 = 0; i0 < ns; i0 += 32)
 		{
-			double2 q = pos[s + i];
-			double m = mass[s + i];
-			double2 wz = make_double2((q.x - cn.x) * ihn, (q.y - cn.y) * ihn);
-			if (p == 0)
+			const int nq = min(32, ns - i0);
+			double mq = 0;
+			double2 iq = make_double2(0, 0), gq = make_double2(0, 0);
+			if (p < nq)
 			{
-				double2 lg = make_double2(log(hypot(wz.x, wz.y)), atan2(-wz.y, -wz.x));
-				v.x += m * lg.x + m * lhn;
-				v.y += m * lg.y;
+				const double2 q = pos[s + i0 + p];
+				mq = mass[s + i0 + p];
+				const double2 wz = make_double2((q.x - cn.x) * ihn, (q.y - cn.y) * ihn);
+				iq = cinv(wz);
+				gq = make_double2(log(hypot(wz.x, wz.y)), atan2(-wz.y, -wz.x));
 			}
-			else
+			for (int i = 0; i < nq; i++)
 			{
-				double2 iw = cinv(wz);
-				double2 t = cpow_int(iw, p);
-				v.x -= m * t.x / p;
-				v.y -= m * t.y / p;
+				const double m = __shfl_sync(0xffffffffu, mq, i);
+				const double2 lg = shfl_c(gq, i);
+				const double2 t = warp_powers(shfl_c(iq, i), p);
+				if (p == 0)
+				{
+					v.x += m * lg.x + m * lhn;
+					v.y += m * lg.y;
+				}
+				else
+				{
+					v.x -= m * t.x * ip;
+					v.y -= m * t.y * ip;
+				}
 			}
 		}
 		r = cadd(r, v);
 	}
-	local[(size_t)n * (P + 1) + p] = r;
+	if (act) local[(size_t)n * (P + 1) + p] = r;
 }
 
 /* leaf records for the solver: centre, 1/h, packed near stars (neighbours
