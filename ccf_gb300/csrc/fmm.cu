@@ -8,9 +8,10 @@ sum c_l ((z - c)/h)^l.  Translations:
   P2M  fmm.cuh:21-49       M2M  fmm.cuh:109-139      L2L  fmm.cuh:204-223
   M2L  fmm.cuh:281-322     P2L  fmm.cuh:387-413
 Layout: one warp per node, lane p computes coefficient p (order <= 31, so a
-whole expansion is one warp).  Each translation is written as a Horner
-recurrence with a single complex reciprocal, instead of the reference's
-division per term.  The binomial table is passed in: by default it holds the
+whole expansion is one warp).  A translation takes one complex reciprocal
+per source, not the reference's division per term; powers come from a
+product scan over the warp, and the M2L sum runs over pre-scaled terms (the
+FP64 pipe is the bound).  The binomial table is passed in: by default it holds the
 reference's int32 Pascal triangle (whose entries above n = 33 wrap), because
 the reference's M2L uses those values and its roots depend on them.
 ******************************************************************************/
