@@ -420,8 +420,10 @@ CCF_D float2 eval_df32(const FieldView& F, int leaf, double2 z, double2 s3_off)
 {
 	float2 s3 = make_float2(0, 0);
 	float2 d2l = make_float2(0, 0);
+	bool folded = false;
 	if (leaf >= 0)
 	{
+		folded = F.leaf_fold != nullptr && F.leaf_fold[leaf];
 		int n = F.leaf_near_count[leaf];
 		const NearStar* ns = F.leaf_near + (size_t)leaf * MAX_NEAR;
 		for (int i = 0; i < n; i++)
@@ -438,7 +440,7 @@ CCF_D float2 eval_df32(const FieldView& F, int leaf, double2 z, double2 s3_off)
 		const int P = F.order;
 		double2 dzd = leaf_dz(F, leaf, z);
 		float2 dz = make_float2((float)dzd.x, (float)dzd.y);
-		const float2* L = F.leaf_loc3f + (size_t)leaf * (P + 1);
+		const float2* L = (folded ? F.leaf_loc3f_fold : F.leaf_loc3f) + (size_t)leaf * (P + 1);
 		float2 acc = L[P];
 		for (int i = P - 1; i >= 3; i--) acc = fadd(fmulc(acc, dz), L[i]);
 		d2l = acc;
@@ -447,7 +449,8 @@ CCF_D float2 eval_df32(const FieldView& F, int leaf, double2 z, double2 s3_off)
 	{
 		s3 = make_float2((float)s3_off.x, (float)s3_off.y);
 	}
-	const float2 d2s = smooth_d2zbar_f32(F, z);
+	/* a folded leaf's block holds the smooth-mass term of f' */
+	const float2 d2s = folded ? make_float2(0.f, 0.f) : smooth_d2zbar_f32(F, z);
 	const float t2 = (float)F.theta2;
 	return make_float2(-2 * t2 * s3.x - d2l.x - d2s.x, -2 * t2 * s3.y - d2l.y + d2s.y);
 }

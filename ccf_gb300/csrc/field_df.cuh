@@ -172,15 +172,20 @@ CCF_D double2 smooth_alpha_any(const FieldView& F, double2 z)
 CCF_D double2 eval_f_df(const FieldView& F, int leaf, double2 z, double cphi, double sphi, const NearSums& ext)
 {
 	double2 s2 = ext.s2, dl = make_double2(0, 0);
+	bool folded = false;
 	if (leaf >= 0)
 	{
 		const SumsDF S = leaf_sums_df<false>(F, leaf, z);
 		const int P = F.order;
 		const dfc dz = leaf_dz_df(F, leaf, z);
-		dl = dfc_to(horner_df(F.leaf_loc_df + ((size_t)leaf * 2 + 1) * (P + 1), P, 2, dz));
+		folded = F.leaf_fold != nullptr && F.leaf_fold[leaf];
+		const float4* L = folded ? F.leaf_loc_df_fold : F.leaf_loc_df;
+		dl = dfc_to(horner_df(L + ((size_t)leaf * 2 + 1) * (P + 1), P, 2, dz));
 		s2 = dfc_to(S.s2);
 	}
-	const double2 ds = smooth_dzbar_any(F, z);
+	/* a leaf with the smooth-mass series folded into its expansion keeps only
+	   the constant of d alpha_s / d zbar */
+	const double2 ds = folded ? make_double2(F.smooth_k1, 0) : smooth_dzbar_any(F, z);
 	const double a = 1 - F.kappa_tot - smooth_dz(F, z);
 	double2 f;
 	f.x = F.shear + F.theta2 * s2.x - dl.x - ds.x - a * cphi;

@@ -412,8 +412,23 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 			   partial sums meet in shared memory.  Tail sweeps with a handful of
 			   active roots then cost 1/S of a full tile on every CTA instead of a
 			   full tile on one CTA. */
+			/* S is chosen for the shortest sweep: a CTA takes ceil(tiles / cluster)
+			   tiles, each costing a fixed ~1/8 (staging, barriers, the step) plus
+			   7/8 of a full tile's sums divided by S; ties keep the smaller S */
 			int S = 1;
-			while (S < NT / 32 && (total + TILE / S - 1) / (TILE / S) < csize) S *= 2;
+			{
+				int best = 1 << 30;
+				for (int s2 = 1; s2 <= NT / 32; s2 *= 2)
+				{
+					const int nt = (total + TILE / s2 - 1) / (TILE / s2);
+					const int cost = ((nt + csize - 1) / csize) * (NT / 32 + 7 * (NT / 32) / s2);
+					if (cost < best)
+					{
+						best = cost;
+						S = s2;
+					}
+				}
+			}
 			const int TT = TILE / S;
 			const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 			const int part = warp % S;
