@@ -205,10 +205,10 @@ class ClockSampler:
 
 # DRAM bytes (read + write) of the continuation launch per continuation point,
 # from the ncu capture summarised in
-# profiles/track_kernel_n2000_salpeter_phi512.md: 88.5 MB for the 4056 * 512
+# profiles/track_kernel_n2000_salpeter_phi512.md: 89.5 MB for the 4056 * 512
 # continuation points of that launch (the 40-byte outputs and the column
 # tables; leaf records and stars stay in L2).  It grows with the points written.
-CONT_DRAM_BYTES_PER_POINT = 88.5e6 / (4056 * 512)
+CONT_DRAM_BYTES_PER_POINT = 89.5e6 / (4056 * 512)
 
 
 def hbm_peak_gbs() -> float | None:
