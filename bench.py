@@ -320,11 +320,11 @@ def run_multi(args) -> None:
                     cs.append(c)
                 return cs
 
-            def one_pass(cs, results=False):
+            def one_pass(cs, results=False, bufs=None):
                 barrier()
                 t0 = time.perf_counter()
                 assert run_batch(cs), cs[0].last_error()
-                out = [c.results(stars=False) for c in cs] if results else None
+                out = [c.results(stars=False, out=b) for c, b in zip(cs, bufs)] if results else None
                 barrier()
                 return time.perf_counter() - t0, out
 
@@ -334,7 +334,10 @@ def run_multi(args) -> None:
             ts = [one_pass(cs)[0] for _ in range(args.steps)]
             t = reduce(statistics.median(ts), MAX)
             pts = reduce(float(sum(c.info()["num_points"] for c in cs)), SUM)
-            te, outs = one_pass(cs, results=True)
+            # page-locked destinations for every field's results, allocated
+            # once outside the timed pass (the copies themselves are timed)
+            bufs = [c.result_buffers(pinned=True) for c in cs]
+            te, outs = one_pass(cs, results=True, bufs=bufs)
             te = reduce(te, MAX)
             d2h = sum(o["ccs"].nbytes + o["caustics"].nbytes + o["errs"].nbytes for o in outs)
             fp = make("fp64")
