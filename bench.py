@@ -237,14 +237,18 @@ def tracker_flops_per_eval(info: dict, approx: int) -> float:
     m/d and m/d^2 sums in double-float, pole and m/d^3 in FP32); the alpha and
     d alpha/d zbar Horner passes over the local expansion; the FP32 f' pass; for
     the rectangular Taylor smooth mass the d alpha/d zbar and alpha series;
-    about 200 for the assembly of f, the step and the bookkeeping."""
+    about 200 for the assembly of f, the step and the bookkeeping.  Leaves
+    with the smooth-mass series folded into their expansion skip the series:
+    it is charged to the unfolded share of the leaves (leaves_folded /
+    num_leaves, the stand-in for the share of evaluations there)."""
     n = info["near_mean"]
     P = info["expansion_order"]
     per = 234.0 * n + 81.0 * (2 * P - 3) + 8.0 * max(P - 3, 0) + 200.0
     if info["rectangular"] and approx:
         ts = info["taylor_smooth"]
         m = (ts - 1) // 2
-        per += 81.0 * (max(m - 1, 0) + ts + 1) + 8.0 * max(m - 1, 0) + 250.0
+        unfolded = 1.0 - info.get("leaves_folded", 0) / max(1, info["num_leaves"])
+        per += (81.0 * (max(m - 1, 0) + ts + 1) + 8.0 * max(m - 1, 0) + 250.0) * unfolded
     return per
 
 

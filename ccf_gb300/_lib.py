@@ -112,6 +112,7 @@ class CcfInfo(ctypes.Structure):
         ("near_mean", ctypes.c_double),
         ("centres_solved", ctypes.c_int),
         ("rows_retracked", ctypes.c_int),
+        ("leaves_folded", ctypes.c_int),
     ]
 
     def as_dict(self) -> dict:

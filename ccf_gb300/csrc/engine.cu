@@ -474,6 +474,7 @@ ccf_status Engine::build_fmm(Field& f)
 	/* smooth-mass polynomials */
 	float4 inv_corner_df = make_float4(0, 0, 0, 0);
 	bool fold_ok = false;
+	std::vector<unsigned char> fold_host;   /* the folded-leaf flags, for ccf_info.leaves_folded */
 	SmoothPoly sp = smooth_polynomials(d.kappa_star, d.corner_x1, d.corner_x2, d.taylor_smooth);
 	{
 		std::vector<double2> d1(std::max(1, sp.m)), d2(std::max(1, sp.m)), a(sp.a.size());
@@ -555,8 +556,11 @@ ccf_status Engine::build_fmm(Field& f)
 				f.fold_coef.ptr + 2 * M + 1, 2 * M, f.fold_coef.ptr + 4 * M + 1, na, 0.95 * std::hypot(d.corner_x1, d.corner_x2),
 				f.leaf_loc_df_fold.ptr, f.leaf_loc3f_fold.ptr, f.leaf_fold.ptr);
 			CCF_TRY(cudaGetLastError(), "fold_smooth_kernel");
+			fold_host.resize(nl);
+			CCF_TRY(cudaMemcpyAsync(fold_host.data(), f.leaf_fold.ptr, nl, cudaMemcpyDeviceToHost, s), "fold");
 		}
 		CCF_TRY(cudaStreamSynchronize(s), "smooth");
+		for (unsigned char v : fold_host) f.info.leaves_folded += v ? 1 : 0;
 	}
 	int lerr = 0;
 	CCF_TRY(cudaMemcpyAsync(&lerr, f.level_out.ptr + 2, sizeof(int), cudaMemcpyDeviceToHost, s), "leaves");

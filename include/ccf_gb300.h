@@ -168,6 +168,9 @@ typedef struct ccf_info
 	int rows_retracked;          /* tracker rows that failed the check and were tracked again
 	                                with sub-steps of 1/8 phi step (rows_rerun: those that
 	                                failed again and went to the full-sum solver) */
+	int leaves_folded;           /* leaves whose expansion carries the smooth-mass Taylor
+	                                series (mixed precision, rectangular Taylor form), so
+	                                that the continuation skips the series there */
 } ccf_info;
 
 typedef struct ccf_handle ccf_handle;
