@@ -1,0 +1,64 @@
+"""Host logic of bench.py on the CPU: the FP32 operation count behind the
+roofline, the seeded batch and serving workloads, and the clock record."""
+import math
+
+import bench
+
+HEADLINE_INFO = dict(near_mean=15.68, expansion_order=23, rectangular=1, taylor_smooth=57, num_leaves=1225)
+
+
+def test_smooth_series_charged_to_unfolded_leaves_only():
+    none = bench.tracker_flops_per_eval(dict(HEADLINE_INFO, leaves_folded=0), approx=1)
+    some = bench.tracker_flops_per_eval(dict(HEADLINE_INFO, leaves_folded=1061), approx=1)
+    every = bench.tracker_flops_per_eval(dict(HEADLINE_INFO, leaves_folded=1225), approx=1)
+    # the base evaluation (near stars, two double-float Horner passes, f' pass, assembly)
+    base = 234.0 * 15.68 + 81.0 * (2 * 23 - 3) + 8.0 * 20 + 200.0
+    assert math.isclose(every, base)
+    assert none > some > every
+    # the series part scales with the unfolded share of the leaves
+    assert math.isclose(some - every, (none - every) * (1225 - 1061) / 1225)
+
+
+def test_no_series_without_the_rectangular_taylor_form():
+    disc = bench.tracker_flops_per_eval(dict(HEADLINE_INFO, rectangular=0, leaves_folded=0), approx=1)
+    exact = bench.tracker_flops_per_eval(dict(HEADLINE_INFO, leaves_folded=0), approx=0)
+    assert math.isclose(disc, exact)
+    assert disc < bench.tracker_flops_per_eval(dict(HEADLINE_INFO, leaves_folded=0), approx=1)
+
+
+def test_batch_fields_are_seeded_and_valid():
+    a, b = bench.batch_fields(), bench.batch_fields()
+    assert a == b and len(a) == 256
+    for i, f in enumerate(a):
+        assert f["random_seed"] == 10000 + i
+        assert 50 <= f["num_stars"] <= 1000
+        assert f["num_phi"] % (2 * f["num_branches"]) == 0   # the reference's validity rule
+        assert not bench._singular(f["kappa_tot"], f["shear"])
+
+
+def test_serving_requests_are_a_seeded_poisson_stream():
+    reqs = bench.serving_requests(64)
+    assert reqs == bench.serving_requests(64)
+    times = [t for t, _ in reqs]
+    assert all(t1 > t0 for t0, t1 in zip(times, times[1:]))
+    assert 0.5 < times[-1] / 64 / 0.05 < 2.0     # mean inter-arrival ~50 ms
+    for _, p in reqs:
+        assert 100 <= p["num_stars"] <= 50000
+        assert p["num_branches"] in (8, 32, 128)
+        assert p["num_phi"] % (2 * p["num_branches"]) == 0
+        assert 1000 <= p["num_phi"] <= 10000 + 2 * p["num_branches"]
+        assert not bench._singular(p["kappa_tot"], p["shear"])
+
+
+def test_clock_summary_parses_samples_and_reasons():
+    c = bench.ClockSampler(0)
+    c.lines = [
+        "0, 2070, 2070, 900.1, 0x0, Not Active, Not Active, Not Active, Not Active",
+        "0, 1980, 2070, 1390.0, 0x4, Not Active, Not Active, Not Active, Active",
+        "garbage",
+    ]
+    s = c.summary()
+    assert s["samples"] == 2 and s["sm_max_mhz"] == 2070.0
+    assert s["sm_mhz"] == (2070.0 + 1980.0) / 2
+    assert s["reasons"] == ["sw_power_cap"]
+    assert bench.ClockSampler(0).summary() == {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
