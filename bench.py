@@ -663,6 +663,7 @@ def main() -> None:
                        "sweeps_step": info["max_sweeps_step"], "root_updates": info["root_updates"],
                        "sum_terms": info["sum_terms"], "rows_rerun": info["rows_rerun"],
                        "step_halvings": info["step_halvings"], "near_mean": info["near_mean"],
+                       "num_leaves": info["num_leaves"], "leaves_folded": info["leaves_folded"],
                        "t_stars": info["t_stars"], "t_tree": info["t_tree"],
                        "t_init_roots": info["t_init_roots"], "t_ccs": info["t_ccs"], "peaks": peaks},
         }
