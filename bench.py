@@ -665,7 +665,12 @@ def main() -> None:
                        "step_halvings": info["step_halvings"], "near_mean": info["near_mean"],
                        "num_leaves": info["num_leaves"], "leaves_folded": info["leaves_folded"],
                        "t_stars": info["t_stars"], "t_tree": info["t_tree"],
-                       "t_init_roots": info["t_init_roots"], "t_ccs": info["t_ccs"], "peaks": peaks},
+                       "t_init_roots": info["t_init_roots"], "t_ccs": info["t_ccs"],
+                       "t_polish": info["t_caustics"], "points_polished": info["points_polished"],
+                       "points_above_target": info["points_above_target"],
+                       "points_at_fp64_floor": info["points_at_fp64_floor"],
+                       "max_error_unpolished": info["max_error_unpolished"],
+                       "unconverged_unpolished": info["unconverged_unpolished"], "peaks": peaks},
         }
         print(json.dumps(line), flush=True)
     if ws > 1:

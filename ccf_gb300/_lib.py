@@ -113,6 +113,11 @@ class CcfInfo(ctypes.Structure):
         ("centres_solved", ctypes.c_int),
         ("rows_retracked", ctypes.c_int),
         ("leaves_folded", ctypes.c_int),
+        ("max_error_unpolished", ctypes.c_double),
+        ("unconverged_unpolished", ctypes.c_longlong),
+        ("points_polished", ctypes.c_longlong),
+        ("points_above_target", ctypes.c_longlong),
+        ("points_at_fp64_floor", ctypes.c_longlong),
     ]
 
     def as_dict(self) -> dict:

@@ -290,8 +290,8 @@ ccf_status Engine::prepare_field(Field& f, int verbose)
 	CCF_TRY(f.errs.ensure(npts), "cudaMalloc(errs)");
 	if (p.write_caustics) CCF_TRY(f.caustics.ensure(npts), "cudaMalloc(caustics)");
 	if (p.write_mu_length_scales) CCF_TRY(f.mu.ensure(npts), "cudaMalloc(mu_length_scales)");
-	CCF_TRY(f.stats.ensure(16), "cudaMalloc(stats)");
-	CCF_TRY(cudaMemsetAsync(f.stats.ptr, 0, 16 * sizeof(unsigned long long), s), "memset");
+	CCF_TRY(f.stats.ensure(STATS_WORDS), "cudaMalloc(stats)");
+	CCF_TRY(cudaMemsetAsync(f.stats.ptr, 0, STATS_WORDS * sizeof(unsigned long long), s), "memset");
 
 	/* info */
 	info.num_stars = N;
@@ -552,9 +552,10 @@ ccf_status Engine::build_fmm(Field& f)
 			CCF_TRY(f.leaf_fold.ensure(nl), "cudaMalloc(fold)");
 			CCF_TRY(f.leaf_loc_df_fold.ensure((size_t)nl * 2 * (P + 1)), "cudaMalloc(fold)");
 			CCF_TRY(f.leaf_loc3f_fold.ensure((size_t)nl * (P + 1)), "cudaMalloc(fold)");
+			CCF_TRY(f.leaf_loc_fold64.ensure((size_t)nl * 3 * (P + 1)), "cudaMalloc(fold)");
 			launch_fold_smooth(s, nl, P, f.leaf_center.ptr, f.leaf_inv_half.ptr, f.leaf_loc.ptr, f.fold_coef.ptr, 2 * M + 1,
 				f.fold_coef.ptr + 2 * M + 1, 2 * M, f.fold_coef.ptr + 4 * M + 1, na, 0.95 * std::hypot(d.corner_x1, d.corner_x2),
-				f.leaf_loc_df_fold.ptr, f.leaf_loc3f_fold.ptr, f.leaf_fold.ptr);
+				f.leaf_loc_df_fold.ptr, f.leaf_loc3f_fold.ptr, f.leaf_loc_fold64.ptr, f.leaf_fold.ptr);
 			CCF_TRY(cudaGetLastError(), "fold_smooth_kernel");
 			fold_host.resize(nl);
 			CCF_TRY(cudaMemcpyAsync(fold_host.data(), f.leaf_fold.ptr, nl, cudaMemcpyDeviceToHost, s), "fold");
@@ -616,6 +617,7 @@ ccf_status Engine::build_fmm(Field& f)
 	V.leaf_fold = fold_ok ? f.leaf_fold.ptr : nullptr;
 	V.leaf_loc_df_fold = fold_ok ? f.leaf_loc_df_fold.ptr : nullptr;
 	V.leaf_loc3f_fold = fold_ok ? f.leaf_loc3f_fold.ptr : nullptr;
+	V.leaf_loc_fold64 = fold_ok ? f.leaf_loc_fold64.ptr : nullptr;
 	CCF_TRY(f.view_dev.ensure(1), "cudaMalloc(view)");
 	CCF_TRY(cudaMemcpyAsync(f.view_dev.ptr, &V, sizeof(V), cudaMemcpyHostToDevice, s), "view");
 	return CCF_OK;
@@ -911,6 +913,33 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		A.num_rows_dev = P.rerun_count.ptr + 3;
 	}
 	CCF_TRY(launch_solve(s, A, mixed, false), "find_ccs");
+	/* FP64 polish of the points above the 1/mu target or left unconverged;
+	   it also forms the largest 1/mu error and the non-finite flag */
+	{
+		long long max_points = 0, total_points = 0;
+		for (Field* f : fields)
+		{
+			const long long n = (long long)f->d.num_roots * f->params.num_branches *
+				(f->params.num_phi / f->params.num_branches + 1);
+			max_points = std::max(max_points, n);
+			total_points += n;
+		}
+		/* room for 1 in 128 points to be listed (points beyond it are polished
+		   by the scan in place) */
+		const long long cap = std::min(1LL << 24, std::max(1LL << 16, total_points / 128));
+		CCF_TRY(P.polish_list.ensure((size_t)cap + 1), "cudaMalloc(polish)");
+		CCF_TRY(cudaMemsetAsync(P.polish_list.ptr, 0, sizeof(unsigned long long), s), "memset");
+		PolishArgs PA;
+		PA.fields = P.views.ptr;
+		PA.outs = P.outs.ptr;
+		PA.num_fields = nf;
+		PA.b0 = PA.nbs = PA.k0 = PA.nks = 0;
+		PA.list_count = P.polish_list.ptr;
+		PA.list = P.polish_list.ptr + 1;
+		PA.list_cap = cap;
+		for (Field* f : fields) CCF_TRY(cudaEventRecord(f->ev[6], s), "event");
+		CCF_TRY(launch_polish(s, PA, max_points, num_sms), "polish");
+	}
 	for (Field* f : fields) CCF_TRY(cudaEventRecord(f->ev[5], s), "event");
 	CCF_TRY(cudaStreamSynchronize(s), "solver");
 
@@ -918,16 +947,22 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 	for (int fi = 0; fi < nf; fi++)
 	{
 		Field* f = fields[fi];
-		unsigned long long st[16];
-		CCF_TRY(cudaMemcpy(st, f->stats.ptr, 16 * sizeof(unsigned long long), cudaMemcpyDeviceToHost), "stats");
+		unsigned long long st[STATS_WORDS];
+		CCF_TRY(cudaMemcpy(st, f->stats.ptr, STATS_WORDS * sizeof(unsigned long long), cudaMemcpyDeviceToHost), "stats");
 		ccf_info& info = f->info;
 		double me;
-		std::memcpy(&me, &st[0], sizeof(double));
+		std::memcpy(&me, &st[STAT_POLISHED_MAX_ERR], sizeof(double));
 		info.max_error = me;
-		info.has_nan = st[1] & 1 ? 1 : 0;
+		std::memcpy(&me, &st[0], sizeof(double));
+		info.max_error_unpolished = me;
+		info.has_nan = st[STAT_POLISHED_NAN] ? 1 : 0;
 		info.root_updates = (long long)st[2];
 		info.sum_terms = (long long)st[3];
-		info.unconverged = (long long)st[4];
+		info.unconverged = (long long)st[STAT_POLISHED_UNCONV];
+		info.unconverged_unpolished = (long long)st[4];
+		info.points_polished = (long long)st[STAT_POLISHED];
+		info.points_above_target = (long long)st[STAT_POLISHED_ABOVE];
+		info.points_at_fp64_floor = (long long)st[STAT_POLISHED_FLOOR];
 		info.max_sweeps_init = (int)st[5];
 		info.max_sweeps_step = (int)st[6];
 		info.root_updates_init = (long long)st[7];
@@ -939,13 +974,13 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		info.t_stars = ev_ms(f->ev[0], f->ev[1]) * 1e-3;
 		info.t_tree = ev_ms(f->ev[1], f->ev[2]) * 1e-3;
 		info.t_init_roots = ev_ms(f->ev[3], f->ev[4]) * 1e-3;
-		info.t_ccs = ev_ms(f->ev[4], f->ev[5]) * 1e-3;
-		info.t_caustics = 0;
+		info.t_ccs = ev_ms(f->ev[4], f->ev[6]) * 1e-3;
+		info.t_caustics = ev_ms(f->ev[6], f->ev[5]) * 1e-3;
 		info.t_total = ev_ms(f->ev[0], f->ev[5]) * 1e-3;
 		/* root seeds, initial solve, continuation (tracker: phase table, item
 		   marking, tracking, row collection, table clearing, re-tracking, row
-		   collection and the full-sum launch for the rows to re-run) */
-		info.kernel_launches += track ? 10 : 3;
+		   collection and the full-sum launch for the rows to re-run), FP64 polish */
+		info.kernel_launches += track ? 12 : 5;
 		info.centres_solved = f->params.num_branches / seg[fi];
 		if (info.has_nan)
 		{

@@ -118,6 +118,7 @@ struct Field
 	DBuf<float2> leaf_loc3f;
 	DBuf<float4> leaf_near_df, leaf_loc_df, leaf_loc_df_fold;
 	DBuf<float2> leaf_mass_df, leaf_ih_df, leaf_loc3f_fold;
+	DBuf<double2> leaf_loc_fold64;
 	DBuf<unsigned char> leaf_fold;
 	DBuf<double2> fold_coef;   /* the conjugated smooth-mass series in z, for the fold */
 	int num_leaves = 0;
@@ -163,6 +164,7 @@ struct SolverPools
 	DBuf<int> item_start;                   /* first tracker work item of each continuation row */
 	DBuf<int2> solo;                        /* tracker roots run alone, and their count after them */
 	DBuf<unsigned char> is_solo;            /* per continuation root */
+	DBuf<unsigned long long> polish_list;   /* [0] count, then the points the FP64 polish works on */
 	DBuf<FieldView> views;
 	DBuf<FieldOut> outs;
 	DBuf<const float4*> hilo_ptrs;

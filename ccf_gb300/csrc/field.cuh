@@ -92,6 +92,7 @@ struct FieldView
 	const unsigned char* leaf_fold;
 	const float4* leaf_loc_df_fold;   /* like leaf_loc_df */
 	const float2* leaf_loc3f_fold;    /* like leaf_loc3f */
+	const double2* leaf_loc_fold64;   /* like leaf_loc, in FP64 (the FP64 polish) */
 };
 
 /* leaf containing z, or -1 when z lies outside the root box (the reference

@@ -450,7 +450,7 @@ CCF_D double fold_tail(const double2* __restrict__ e, int n, double2 z0, double 
 __global__ void fold_smooth_kernel(int num_leaves, int P, const double2* __restrict__ leaf_center,
 	const double* __restrict__ leaf_inv_half, const double2* __restrict__ loc, const double2* __restrict__ ef, int nf,
 	const double2* __restrict__ er, int nr, const double2* __restrict__ eq, int nq, double radius,
-	float4* __restrict__ loc_df, float2* __restrict__ loc3f, unsigned char* __restrict__ fold)
+	float4* __restrict__ loc_df, float2* __restrict__ loc3f, double2* __restrict__ loc64, unsigned char* __restrict__ fold)
 {
 	__shared__ double inv[FOLD_MAXD + 1];
 	for (int k = threadIdx.x; k <= FOLD_MAXD; k += blockDim.x) inv[k] = k ? 1.0 / k : 0.0;
@@ -496,16 +496,22 @@ __global__ void fold_smooth_kernel(int num_leaves, int P, const double2* __restr
 	loc_df[((size_t)l * 2 + 0) * (P + 1) + i] = make_float4(x0.x, y0.x, x0.y, y0.y);
 	loc_df[((size_t)l * 2 + 1) * (P + 1) + i] = make_float4(x1.x, y1.x, x1.y, y1.y);
 	loc3f[(size_t)l * (P + 1) + i] = make_float2((float)a2.x, (float)a2.y);
+	if (loc64)
+	{
+		loc64[((size_t)l * 3 + 0) * (P + 1) + i] = a0;
+		loc64[((size_t)l * 3 + 1) * (P + 1) + i] = a1;
+		loc64[((size_t)l * 3 + 2) * (P + 1) + i] = a2;
+	}
 }
 
 void launch_fold_smooth(cudaStream_t s, int num_leaves, int P, const double2* leaf_center, const double* leaf_inv_half,
 	const double2* loc, const double2* ef, int nf, const double2* er, int nr, const double2* eq, int nq, double radius,
-	float4* loc_df, float2* loc3f, unsigned char* fold)
+	float4* loc_df, float2* loc3f, double2* loc64, unsigned char* fold)
 {
 	if (num_leaves <= 0) return;
 	const int warps = 4;
 	fold_smooth_kernel<<<(num_leaves + warps - 1) / warps, warps * 32, 0, s>>>(num_leaves, P, leaf_center, leaf_inv_half, loc, ef, nf, er,
-		nr, eq, nq, radius, loc_df, loc3f, fold);
+		nr, eq, nq, radius, loc_df, loc3f, loc64, fold);
 }
 
 } /* namespace ccf */

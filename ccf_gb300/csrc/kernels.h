@@ -81,12 +81,48 @@ struct FieldOut
 	float4* cont_snap32;
 	double2* cont_snap64;
 	/* statistics */
-	unsigned long long* stats;   /* [0] max_err bits, [1] nan flag, [2] updates, [3] terms,
-	                                [4] unconverged, [5] max sweeps init, [6] max sweeps step,
-	                                [7] updates in the initial solve, [8] terms in the initial solve,
-	                                [9] continuation rows re-run by the full-sum solver, [10] tracker
-	                                sub-step halvings, [11] TRACK_* flags of the re-run rows,
-	                                [12] rows tracked again with fine sub-steps */
+	unsigned long long* stats;   /* STATS_WORDS words: [0] max_err bits, [1] nan flag, [2] updates,
+	                                [3] terms, [4] unconverged, [5] max sweeps init, [6] max sweeps
+	                                step, [7] updates in the initial solve, [8] terms in the initial
+	                                solve, [9] continuation rows re-run by the full-sum solver, [10]
+	                                tracker sub-step halvings, [11] TRACK_* flags of the re-run rows,
+	                                [12] rows tracked again with fine sub-steps; [16] .. [20] the
+	                                FP64 polish (STAT_POLISHED_*) */
+};
+
+/* statistics words of a field (FieldOut::stats) */
+constexpr int STATS_WORDS = 24;
+constexpr int STAT_POLISHED_MAX_ERR = 16;   /* largest 1/mu error after the polish (double bits) */
+constexpr int STAT_POLISHED_NAN = 17;       /* a non-finite 1/mu error after the polish */
+constexpr int STAT_POLISHED = 18;           /* points the polish worked on */
+constexpr int STAT_POLISHED_UNCONV = 19;    /* unconverged points the polish could not converge */
+constexpr int STAT_POLISHED_ABOVE = 20;     /* polished points whose 1/mu error stays above POLISH_ERR with
+                                               |f| above the FP64 floor (below) */
+constexpr int STAT_POLISHED_FLOOR = 21;     /* polished points above POLISH_ERR at the FP64 floor: |f| within
+                                               four times |f'| times half the FP64 spacing of the root, which no
+                                               FP64 root can improve on */
+
+/* FP64 polish (polish.cu) */
+constexpr double POLISH_ERR = 0.000000001;       /* the reference's 1/mu target (include/ccf_functions.cuh:207-211) */
+constexpr double POLISH_STEP_TOL = 0.000000001;  /* theta_star: the reference's step test (ccf_functions.cuh:385) */
+constexpr double POLISH_MOVE = 1e-4;             /* theta_star: the most a converged, flagged point may move */
+constexpr double POLISH_MOVE_LISTED = 1e-2;      /* theta_star: the same for an unconverged point */
+
+/* The solvers store -1 - err in the 1/mu slot of a point they left
+   unconverged; the polish, which always follows them, removes the mark. */
+CCF_HD double unconverged_mark(double err) { return isfinite(err) && err >= 0 ? -1 - err : err; }
+
+/* the fields of a polish launch: every point of every field, or (nbs > 0)
+   the columns [k0, k0 + nks) of branches [b0, b0 + nbs) */
+struct PolishArgs
+{
+	const FieldView* fields;
+	const FieldOut* outs;
+	int num_fields;
+	int b0, nbs, k0, nks;
+	unsigned long long* list;        /* flagged points: field << 48 | output slot */
+	unsigned long long* list_count;  /* zeroed before the launch */
+	long long list_cap;
 };
 
 /* Outputs of step j of the continuation row (c, side).  Global step
@@ -222,7 +258,7 @@ void launch_leaf_df(cudaStream_t s, int num_leaves, int P, const double2* leaf_c
 	float2* ih_df);
 void launch_fold_smooth(cudaStream_t s, int num_leaves, int P, const double2* leaf_center, const double* leaf_inv_half,
 	const double2* loc, const double2* ef, int nf, const double2* er, int nr, const double2* eq, int nq, double radius,
-	float4* loc_df, float2* loc3f, unsigned char* fold);
+	float4* loc_df, float2* loc3f, double2* loc64, unsigned char* fold);
 
 /* solver.cu */
 int solver_blocks_per_sm(bool mixed);
@@ -234,5 +270,9 @@ cudaError_t launch_collect_rerun(cudaStream_t s, const TrackArgs& a, RowDesc* re
 cudaError_t launch_clear_tables(cudaStream_t s, const TrackArgs& a);
 cudaError_t launch_eval_points(cudaStream_t s, const FieldView* F_dev, int npts, const double2* z, const double* phi,
 	double2* f, double2* df, double2* w, double* err, double* mu);
+
+/* polish.cu: two launches (scan, list) on s; max_points = the largest field's
+   point count (or box); list_count must be zero when they start */
+cudaError_t launch_polish(cudaStream_t s, const PolishArgs& a, long long max_points, int num_sms);
 
 } /* namespace ccf */

@@ -16,7 +16,11 @@ rejected with CCF_ERR_INVALID_ARGUMENT.
 
 All calls share the one array and it keeps the last call's contents; calls
 whose work overlaps on the GPU (two streams, or two host threads) race on it
-and must be serialised by the caller.
+and must be serialised by the caller.  The launch descriptors reach the
+scratch through the parameters of a small set-up kernel enqueued on the
+caller's stream, so a call reads no host memory after it returns.  The
+continuation is followed by the same FP64 polish as ccf_run (polish.cu) over
+the columns this call wrote.
 ******************************************************************************/
 #include "../../include/ccf_gb300.h"
 #include "engine.h"
@@ -39,7 +43,9 @@ unsigned char* g_scratch_addr[MAX_DEVICES] = {};
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-/* device address of the scratch on the current device, looked up once */
+/* device address of the scratch on the current device, looked up once per
+   device (a cudaDeviceReset by the caller invalidates it: the entry point is
+   documented as needing the context it first ran in) */
 cudaError_t scratch_address(int dev, unsigned char** out)
 {
 	std::lock_guard<std::mutex> lock(g_setup_mutex);
@@ -53,6 +59,24 @@ cudaError_t scratch_address(int dev, unsigned char** out)
 	}
 	*out = g_scratch_addr[dev];
 	return cudaSuccess;
+}
+
+/* writes the launch descriptors into the scratch and clears the statistics:
+   everything arrives as kernel parameters, none of it from host memory */
+__global__ void noalloc_setup_kernel(const ccf::FieldView v, const ccf::FieldOut o, const ccf::RowDesc r, const float4* hilo,
+	unsigned char* base, size_t o_view, size_t o_out, size_t o_row, size_t o_hilo, size_t o_stats, size_t o_plist)
+{
+	if (blockIdx.x == 0 && threadIdx.x == 0) *(unsigned long long*)(base + o_plist) = 0;   /* polish list count */
+	if (blockIdx.x != 0) return;
+	if (threadIdx.x == 0)
+	{
+		*(ccf::FieldView*)(base + o_view) = v;
+		*(ccf::FieldOut*)(base + o_out) = o;
+		*(ccf::RowDesc*)(base + o_row) = r;
+		*(const float4**)(base + o_hilo) = hilo;
+	}
+	unsigned long long* st = (unsigned long long*)(base + o_stats);
+	for (int i = threadIdx.x; i < ccf::STATS_WORDS; i += blockDim.x) st[i] = 0;
 }
 
 } /* namespace */
@@ -92,23 +116,31 @@ extern "C" ccf_status ccf_continue_branch_noalloc(ccf_handle* h, int branch, int
 	const size_t o_row = align256(o_out + sizeof(ccf::FieldOut));
 	const size_t o_hilo = align256(o_row + sizeof(ccf::RowDesc));
 	const size_t o_stats = align256(o_hilo + sizeof(const float4*));
-	const size_t o_master = align256(o_stats + 16 * sizeof(unsigned long long));
+	const size_t o_master = align256(o_stats + ccf::STATS_WORDS * sizeof(unsigned long long));
 	const size_t o_snap = align256(o_master + (size_t)R * sizeof(double2));
 	const size_t o_fin = align256(o_snap + (size_t)R * (mixed ? sizeof(float4) : sizeof(double2)));
 	const size_t o_list = align256(o_fin + (size_t)R);
 	const size_t o_fval = align256(o_list + (size_t)R * sizeof(int));
-	const size_t need = align256(o_fval + 2 * (size_t)R * sizeof(double2));
+	const size_t o_plist = align256(o_fval + 2 * (size_t)R * sizeof(double2));
+	const size_t need = o_plist + 256;
 	if (need > NOALLOC_SCRATCH_BYTES)
 	{
 		ccf_internal_set_error(h, "Error. A row of " + std::to_string(R) + " roots needs " + std::to_string(need) +
 			" bytes of scratch; ccf_continue_branch_noalloc has " + std::to_string(NOALLOC_SCRATCH_BYTES) + ".");
 		return CCF_ERR_INVALID_ARGUMENT;
 	}
-	cudaError_t e = cudaSetDevice(eng.device);
+	/* the caller's current device is put back before returning */
+	int caller_dev = -1;
+	cudaError_t e = cudaGetDevice(&caller_dev);
+	if (e == cudaSuccess && caller_dev != eng.device) e = cudaSetDevice(eng.device);
+	auto restore = [&]() {
+		if (caller_dev >= 0 && caller_dev != eng.device) cudaSetDevice(caller_dev);
+	};
 	unsigned char* base = nullptr;
 	if (e == cudaSuccess) e = scratch_address(eng.device, &base);
 	if (e != cudaSuccess)
 	{
+		restore();
 		ccf_internal_set_error(h, std::string("CUDA error in ccf_continue_branch_noalloc setup: ") + cudaGetErrorString(e));
 		return CCF_ERR_CUDA;
 	}
@@ -139,11 +171,8 @@ extern "C" ccf_status ccf_continue_branch_noalloc(ccf_handle* h, int branch, int
 	r.cont_base = 0;
 	const float4* hilo = mixed ? f.star_hilo.ptr : nullptr;
 
-	if (e == cudaSuccess) e = cudaMemcpyAsync(base + o_view, &f.view, sizeof(f.view), cudaMemcpyHostToDevice, s);
-	if (e == cudaSuccess) e = cudaMemcpyAsync(base + o_out, &o, sizeof(o), cudaMemcpyHostToDevice, s);
-	if (e == cudaSuccess) e = cudaMemcpyAsync(base + o_row, &r, sizeof(r), cudaMemcpyHostToDevice, s);
-	if (e == cudaSuccess) e = cudaMemcpyAsync(base + o_hilo, &hilo, sizeof(hilo), cudaMemcpyHostToDevice, s);
-	if (e == cudaSuccess) e = cudaMemsetAsync(base + o_stats, 0, 16 * sizeof(unsigned long long), s);
+	noalloc_setup_kernel<<<1, 32, 0, s>>>(f.view, o, r, hilo, base, o_view, o_out, o_row, o_hilo, o_stats, o_plist);
+	e = cudaGetLastError();
 	if (e == cudaSuccess) e = cudaMemcpyAsync(base + o_master, start_roots, (size_t)R * sizeof(double2), cudaMemcpyDeviceToDevice, s);
 	if (e == cudaSuccess)
 	{
@@ -153,6 +182,7 @@ extern "C" ccf_status ccf_continue_branch_noalloc(ccf_handle* h, int branch, int
 	if (e == cudaSuccess) e = cudaGetLastError();
 	if (e != cudaSuccess)
 	{
+		restore();
 		ccf_internal_set_error(h, std::string("CUDA error in ccf_continue_branch_noalloc: ") + cudaGetErrorString(e));
 		return CCF_ERR_CUDA;
 	}
@@ -174,6 +204,24 @@ extern "C" ccf_status ccf_continue_branch_noalloc(ccf_handle* h, int branch, int
 	A.star_hilo = (const float4* const*)(base + o_hilo);
 	A.error = nullptr;
 	e = ccf::launch_solve(s, A, mixed, false);
+	if (e == cudaSuccess)
+	{
+		/* the FP64 polish of ccf_run, over the columns written here */
+		ccf::PolishArgs PA;
+		PA.fields = A.fields;
+		PA.outs = A.outs;
+		PA.num_fields = 1;
+		PA.b0 = branch;
+		PA.nbs = 1;
+		PA.k0 = side == 0 ? half - num_steps : half + 1;
+		PA.nks = num_steps;
+		/* the rest of the scratch lists the points to polish (count first) */
+		PA.list_count = (unsigned long long*)(base + o_plist);
+		PA.list = PA.list_count + 32;
+		PA.list_cap = (long long)((NOALLOC_SCRATCH_BYTES - o_plist) / sizeof(unsigned long long)) - 32;
+		e = ccf::launch_polish(s, PA, (long long)R * num_steps, eng.num_sms);
+	}
+	restore();
 	if (e != cudaSuccess)
 	{
 		ccf_internal_set_error(h, std::string("CUDA error in ccf_continue_branch_noalloc launch: ") + cudaGetErrorString(e));

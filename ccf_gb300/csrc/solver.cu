@@ -204,7 +204,7 @@ constexpr size_t NO_SLOT = ~(size_t)0;
 
 template <bool DF>
 __device__ __noinline__ bool point_epilogue_warp(const FieldView& F, const FieldOut& O, bool valid, double2 z, int leaf,
-	bool have_off, NearSums off, size_t out, size_t out2, double cphi, double sphi, double* maxerr)
+	bool have_off, NearSums off, size_t out, size_t out2, double cphi, double sphi, double* maxerr, bool unconv)
 {
 	NearSums ns = have_off ? off : zero_sums();
 	const bool mu = O.mu != nullptr;
@@ -218,14 +218,16 @@ __device__ __noinline__ bool point_epilogue_warp(const FieldView& F, const Field
 	else if (O.caustics) pr = eval_point<true, false>(F, leaf, z, cphi, sphi, ns);
 	else if (mu) pr = eval_point<false, true>(F, leaf, z, cphi, sphi, ns);
 	else pr = eval_point<false, false>(F, leaf, z, cphi, sphi, ns);
+	/* an unconverged point is marked for the FP64 polish (polish.cu) */
+	const double stored = unconv ? unconverged_mark(pr.err) : pr.err;
 	O.ccs[out] = z;
-	O.errs[out] = pr.err;
+	O.errs[out] = stored;
 	if (O.caustics) O.caustics[out] = pr.w;
 	if (mu) O.mu[out] = pr.mu_length;
 	if (out2 != NO_SLOT)
 	{
 		O.ccs[out2] = z;
-		O.errs[out2] = pr.err;
+		O.errs[out2] = stored;
 		if (O.caustics) O.caustics[out2] = pr.w;
 		if (mu) O.mu[out2] = pr.mu_length;
 	}
@@ -655,9 +657,11 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 			const size_t out = ((size_t)(v ? a : 0) * nb + ob[0]) * sO.cols + ok[0];
 			const size_t out2 = nslot > 1 ? ((size_t)(v ? a : 0) * nb + ob[1]) * sO.cols + ok[1] : NO_SLOT;
 			const NearSums off = slot >= 0 ? s_offs[slot] : zero_sums();
-			if (!point_epilogue_warp<MIXED>(F, sO, v, z, leaf, slot >= 0, off, out, out2, cphi, sphi, &s_maxerr)) s_nan_err = 1;
+			const bool unconv = v && fin[a] != 1;
+			if (!point_epilogue_warp<MIXED>(F, sO, v, z, leaf, slot >= 0, off, out, out2, cphi, sphi, &s_maxerr, unconv))
+				s_nan_err = 1;
 			if (!v) continue;
-			if (fin[a] != 1) atomicAdd(&s_unconv, 1ull);
+			if (unconv) atomicAdd(&s_unconv, 1ull);
 			if (initial)
 			{
 				long long cb = sR.cont_base;
@@ -1221,7 +1225,7 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 
 			/* the lane's decision; an output step that converged is written
 			   here (mixed precision) or by the direct epilogue below */
-			bool emit = false;
+			bool emit = false, stuck = false;
 			double2 zf = make_double2(0, 0);
 			size_t out = 0, out2 = NO_SLOT;
 			double ecp = 0, esp = 0;
@@ -1263,7 +1267,11 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 					   counts a root that reaches its sweep cap */
 					fail = false;
 					conv = true;
-					if (tt == j * TSUB) unconv++;
+					if (tt == j * TSUB)
+					{
+						unconv++;
+						stuck = true;
+					}
 				}
 				int tn = tt;
 				if (conv)
@@ -1319,13 +1327,15 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 								wv.y -= av * step.y - gx * step.y + gy * step.x;
 								const double af = e.af;
 								const double err = fmax(fabs(af * (af + 2 * av)), fabs(af * (af - 2 * av)));
+								/* a stalled root is marked for the FP64 polish (polish.cu) */
+								const double stored = stuck ? unconverged_mark(err) : err;
 								O.ccs[out] = zf;
-								O.errs[out] = err;
+								O.errs[out] = stored;
 								if (O.caustics) O.caustics[out] = wv;
 								if (out2 != NO_SLOT)
 								{
 									O.ccs[out2] = zf;
-									O.errs[out2] = err;
+									O.errs[out2] = stored;
 									if (O.caustics) O.caustics[out2] = wv;
 								}
 								if (isfinite(err)) atomicMax((unsigned long long*)&s_maxerr[w], (unsigned long long)__double_as_longlong(err));
@@ -1387,7 +1397,8 @@ __global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
 					double2 r2;
 					leafo = (leaf >= 0 && in_leaf_box(F, leaf, zf, r2)) ? leaf : find_leaf(F, zf);
 				}
-				if (!point_epilogue_warp<MIXED>(F, O, emit_direct, zf, leafo, false, zero_sums(), out, out2, ecp, esp, &s_maxerr[w]))
+				if (!point_epilogue_warp<MIXED>(F, O, emit_direct, zf, leafo, false, zero_sums(), out, out2, ecp, esp, &s_maxerr[w],
+						stuck))
 					flags |= (unsigned)TRACK_NONFINITE;
 			}
 		}

@@ -24,7 +24,7 @@ cannot afford).
 extern "C" {
 #endif
 
-#define CCF_GB300_ABI_VERSION 1
+#define CCF_GB300_ABI_VERSION 2
 
 /* Status codes.  The reference returns bool from every stage and prints the
    reason to std::cerr (include/ccf.cuh:1265-1287); here the reason is kept
@@ -57,11 +57,15 @@ typedef enum ccf_precision
 typedef enum ccf_continuation
 {
 	CCF_CONTINUATION_TRACK = 0,  /* default: every root follows its own path in
-	                                phi with a secant predictor and a corrector
-	                                whose Aberth correction keeps the poles of the
-	                                leaf's near stars only; every column is checked
-	                                for two roots on one zero, and a row that fails
-	                                the check (or loses a root) is run again by the
+	                                phi with a quartic predictor (the polynomial
+	                                through its last five positions; the secant
+	                                after sub-steps) and a corrector whose Aberth
+	                                correction keeps the poles of the leaf's near
+	                                stars only; every column is checked for two
+	                                roots on one zero.  A row that fails the check
+	                                (or loses a root) is tracked again from its
+	                                centre with sub-steps of at most 1/8 phi step,
+	                                and a row that fails again is run by the
 	                                full-sum continuation */
 	CCF_CONTINUATION_ABERTH = 1  /* the full Aberth step of the reference for every
 	                                root of a row (include/ccf_functions.cuh:261-394) */
@@ -141,18 +145,21 @@ typedef struct ccf_info
 	double mean_mass_actual;
 	double mean_mass2_actual;
 	double mean_mass2_ln_mass_actual;
-	double max_error;            /* max_error_1/mu */
+	double max_error;            /* max_error_1/mu, after the FP64 polish */
 	long long num_points;        /* num_roots * (num_phi + num_branches) */
 	long long root_updates;      /* executed Aberth updates */
 	long long sum_terms;         /* executed reciprocal-sum terms */
-	long long unconverged;       /* points whose sweep cap was reached */
+	long long unconverged;       /* output points the solvers left unconverged (sweep cap
+	                                reached, tracker stalled) that the FP64 polish could not
+	                                converge either */
 	int max_sweeps_init;         /* most sweeps any branch centre needed */
 	int max_sweeps_step;         /* most sweeps any phi step needed */
 	double t_stars;              /* seconds, CUDA events */
 	double t_tree;               /* tree build + FMM coefficients */
 	double t_init_roots;
 	double t_ccs;
-	double t_caustics;           /* residual, caustic map, length scales */
+	double t_caustics;           /* the FP64 polish (the residual, caustic map and length
+	                                scales are formed in the solvers' epilogues) */
 	double t_total;              /* star generation -> caustics on the device */
 	long long kernel_launches;   /* CUDA kernels this field's run launched */
 	long long root_updates_init; /* the part of root_updates done at the branch centres */
@@ -171,6 +178,19 @@ typedef struct ccf_info
 	int leaves_folded;           /* leaves whose expansion carries the smooth-mass Taylor
 	                                series (mixed precision, rectangular Taylor form), so
 	                                that the continuation skips the series there */
+	/* FP64 polish: every output point whose 1/mu error is above 1e-9, or that
+	   the solvers left unconverged, takes FP64 Newton steps with the near-pole
+	   Aberth correction until the reference's stopping rules hold
+	   (include/ccf_functions.cuh:207-211, :385) */
+	double max_error_unpolished;       /* max_error_1/mu before the polish */
+	long long unconverged_unpolished;  /* unconverged points before the polish */
+	long long points_polished;         /* points the polish worked on */
+	long long points_above_target;     /* polished points whose FP64 1/mu error stays above
+	                                      1e-9 although |f| is above the FP64 floor (below) */
+	long long points_at_fp64_floor;    /* polished points whose 1/mu error stays above 1e-9
+	                                      because |f| is within four times |f'| times half the
+	                                      FP64 spacing of the root: no FP64 root does better (the
+	                                      reference's own FP64 roots carry the same floor) */
 } ccf_info;
 
 typedef struct ccf_handle ccf_handle;
@@ -271,10 +291,16 @@ ccf_status ccf_eval_points(ccf_handle* h, int n, const double* z, const double* 
    start_roots: num_roots complex roots (device memory) at the branch centre.
    ccs, errs, caustics: device arrays in the ccf_get_results layout of the
    field; only the columns of steps 1..num_steps on this side are written
-   (caustics may be NULL).  stream: a cudaStream_t, or NULL for the default
-   stream; the call only enqueues work on it.  The first call on a device
-   looks up the scratch's device address; make that first call before any
-   stream capture.  All calls share the scratch and it keeps the last call's
+   (caustics may be NULL), after the same FP64 polish as ccf_run.  errs holds
+   each written point's 1/mu error: a point meets the reference's target when
+   it is at most 1e-9; the run's statistics are not returned.  stream: a
+   cudaStream_t, or NULL for the default stream; the call only enqueues work
+   on it and reads no host memory once it has returned.  The caller's
+   current device is unchanged on return.  The first call on a device looks
+   up the scratch's device address; make that first call before any stream
+   capture.  The address stays valid for the CUDA context it was looked up
+   in: after a cudaDeviceReset the entry point must not be called again in
+   that process.  All calls share the scratch and it keeps the last call's
    contents: calls whose work overlaps on the GPU race and must be
    serialised by the caller. */
 ccf_status ccf_continue_branch_noalloc(ccf_handle* h, int branch, int side, int num_steps, const double* start_roots,

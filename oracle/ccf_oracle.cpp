@@ -1023,6 +1023,35 @@ int sweep_row(const Field& F, Cx* row, int nroots, char* fin, double phi, bool e
 	return active;
 }
 
+/* The same Aberth step (include/ccf_functions.cuh:193-243) applied to every
+   root of the row from the row as it stood before the sweep, the roots split
+   over nt threads (Jacobi order; the reference updates in place while other
+   threads read, include/ccf_functions.cuh:374-389). */
+int sweep_row_jacobi(const Field& F, Cx* row, int nroots, char* fin, double phi, bool early_out, double tol, int nt,
+	long long& updates, long long& terms)
+{
+	std::vector<Cx> next(row, row + nroots);
+	int active = 0;
+	long long u = 0, t = 0;
+#pragma omp parallel for num_threads(nt) schedule(dynamic, 16) reduction(+ : active, u, t)
+	for (int a = 0; a < nroots; a++)
+	{
+		if (fin[a]) continue;
+		long long ta = 0;
+		Cx res = aberth_update(F, a, row[a], phi, row, nroots, early_out, ta);
+		t += ta;
+		u++;
+		double norm = cabs(sub(res, row[a])) / F.theta;
+		if (norm < tol) fin[a] = 1;
+		else active++;
+		next[a] = res;
+	}
+	std::copy(next.begin(), next.end(), row);
+	updates += u;
+	terms += t;
+	return active;
+}
+
 inline double center_phi(int c, int nb) { return PI / nb + c * 2 * PI / nb; }   /* ccf_functions.cuh:344 */
 
 struct Run
@@ -1354,6 +1383,16 @@ int oracle_run(const oracle_params* p, oracle_info* info, double* stars_out,
 	const int nphi = p->num_phi, nb = p->num_branches;
 	const int half = nphi / (2 * nb);
 	const int nb_solve = (p->max_branches > 0 && p->max_branches < nb) ? p->max_branches : nb;
+	/* the solved branches: first_branch + i branch_stride (all of them by default) */
+	std::vector<int> branch_of(nb_solve);
+	std::vector<char> solved_branch(nb, 0);
+	for (int i = 0; i < nb_solve; i++)
+	{
+		const int st = p->branch_stride > 0 ? p->branch_stride : 1;
+		branch_of[i] = nb_solve == nb ? i : (((p->first_branch + i * st) % nb) + nb) % nb;
+		solved_branch[branch_of[i]] = 1;
+	}
+	const bool jac = p->jacobi != 0;
 	const int nsteps = (p->max_steps > 0 && p->max_steps < half) ? p->max_steps : half;
 	const int nt = std::max(1, p->num_threads);
 	const size_t npts = (size_t)(nphi + nb) * nroots;
@@ -1384,25 +1423,28 @@ int oracle_run(const oracle_params* p, oracle_info* info, double* stars_out,
 	long long upd = 0, terms = 0;
 	/* include/ccf.cuh:906-940: at j = 0 both sides sweep the same centre row */
 	double t0 = now_s();
-#pragma omp parallel for num_threads(nt) schedule(dynamic, 1) reduction(+ : upd, terms)
-	for (int c = 0; c < nb_solve; c++)
+#pragma omp parallel for num_threads(jac ? 1 : nt) schedule(dynamic, 1) reduction(+ : upd, terms)
+	for (int ci = 0; ci < nb_solve; ci++)
 	{
+		const int c = branch_of[ci];
 		Cx* row = &z[center_row(c) * nroots];
 		double phi = center_phi(c, nb);
 		for (int it = 0; it < p->init_iters; it++)
 		{
 			for (int b = 0; b < 2; b++)
 			{
-				sweep_row(F, row, nroots, &fin[((size_t)c * 2 + b) * nroots], phi, early, tol, upd, terms);
+				char* fl = &fin[((size_t)c * 2 + b) * nroots];
+				if (jac) sweep_row_jacobi(F, row, nroots, fl, phi, early, tol, nt, upd, terms);
+				else sweep_row(F, row, nroots, fl, phi, early, tol, upd, terms);
 			}
 		}
 	}
 	double t1 = now_s();
 	/* include/ccf.cuh:1001-1033 with ccf_functions.cuh:261-295 and :321-394 */
-#pragma omp parallel for num_threads(nt) schedule(dynamic, 1) reduction(+ : upd, terms)
+#pragma omp parallel for num_threads(jac ? 1 : nt) schedule(dynamic, 1) reduction(+ : upd, terms)
 	for (int cb = 0; cb < 2 * nb_solve; cb++)
 	{
-		int c = cb / 2, b = cb % 2;
+		int c = branch_of[cb / 2], b = cb % 2;
 		int sgn = (b == 0 ? -1 : 1);
 		char* fn = &fin[((size_t)c * 2 + b) * nroots];
 		for (int j = 1; j <= nsteps; j++)
@@ -1411,21 +1453,50 @@ int oracle_run(const oracle_params* p, oracle_info* info, double* stars_out,
 			const Cx* prev = &z[(center_row(c) + sgn * (j - 1)) * nroots];
 			for (int a = 0; a < nroots; a++) { row[a] = prev[a]; fn[a] = 0; }
 			double phi = center_phi(c, nb) + sgn * (2 * PI / nphi * j);
-			for (int it = 0; it < p->step_iters; it++) sweep_row(F, row, nroots, fn, phi, early, tol, upd, terms);
+			for (int it = 0; it < p->step_iters; it++)
+			{
+				if (jac) sweep_row_jacobi(F, row, nroots, fn, phi, early, tol, nt, upd, terms);
+				else sweep_row(F, row, nroots, fn, phi, early, tol, upd, terms);
+			}
 		}
 	}
 	double t2 = now_s();
 
 	/* optional polish: every (branch, step) row iterated without the early
 	   return until each root's step is below polish_tol */
-	if (p->polish_tol > 0)
+	if (p->polish_tol > 0 && p->polish_newton)
 	{
-#pragma omp parallel for num_threads(nt) schedule(dynamic, 1)
+		/* every solved point alone: FP64 Newton on the oracle's own f and f'
+		   (include/ccf_functions.cuh:69-121) until the step is below
+		   polish_tol theta_star */
+#pragma omp parallel for num_threads(nt) schedule(dynamic, 256)
+		for (long long q = 0; q < (long long)npts; q++)
+		{
+			const int r = (int)(q / nroots);
+			const int c = r / (nphi / nb + 1), k = r % (nphi / nb + 1);
+			const int jj = k - half;
+			if (!solved_branch[c] || jj < -nsteps || jj > nsteps) continue;
+			const double phi = center_phi(c, nb) + (jj < 0 ? -1 : 1) * (2 * PI / nphi * std::abs(jj));
+			Cx zz = z[q];
+			for (int it = 0; it < p->polish_max_iters; it++)
+			{
+				const Node& n = nearest_node(F, zz);
+				const Cx step = div(parametric_cc(F, zz, n, phi), d_parametric_cc_dz(F, zz, n));
+				if (!(std::isfinite(step.re) && std::isfinite(step.im))) break;
+				zz = sub(zz, step);
+				if (cabs(step) < p->polish_tol * F.theta) break;
+			}
+			z[q] = zz;
+		}
+	}
+	else if (p->polish_tol > 0)
+	{
+#pragma omp parallel for num_threads(jac ? 1 : nt) schedule(dynamic, 1)
 		for (int r = 0; r < nphi + nb; r++)
 		{
 			int c = r / (nphi / nb + 1);
 			int k = r % (nphi / nb + 1);
-			if (c >= nb_solve) continue;
+			if (!solved_branch[c]) continue;
 			int jj = k - half;
 			if (jj < -nsteps || jj > nsteps) continue;
 			double phi = center_phi(c, nb) + (jj < 0 ? -1 : 1) * (2 * PI / nphi * std::abs(jj));
@@ -1433,7 +1504,10 @@ int oracle_run(const oracle_params* p, oracle_info* info, double* stars_out,
 			long long u = 0, t = 0;
 			for (int it = 0; it < p->polish_max_iters; it++)
 			{
-				if (sweep_row(F, &z[(size_t)r * nroots], nroots, fl.data(), phi, false, p->polish_tol, u, t) == 0) break;
+				Cx* row = &z[(size_t)r * nroots];
+				const int left = jac ? sweep_row_jacobi(F, row, nroots, fl.data(), phi, false, p->polish_tol, nt, u, t)
+				                     : sweep_row(F, row, nroots, fl.data(), phi, false, p->polish_tol, u, t);
+				if (left == 0) break;
 			}
 		}
 	}
@@ -1450,7 +1524,7 @@ int oracle_run(const oracle_params* p, oracle_info* info, double* stars_out,
 		int r = (int)(q / nroots), a = (int)(q % nroots);
 		int c = r / cols, k = r % cols;
 		int jj = k - half;
-		bool solved = c < nb_solve && jj >= -nsteps && jj <= nsteps;
+		bool solved = solved_branch[c] && jj >= -nsteps && jj <= nsteps;
 		Cx zz = z[q];
 		size_t out = ((size_t)a * nb + c) * cols + k;
 		if (ccs) { ccs[2 * out] = zz.re; ccs[2 * out + 1] = zz.im; }

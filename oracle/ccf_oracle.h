@@ -62,7 +62,20 @@ typedef struct oracle_params
 	                         int32 Pascal table */
 	int max_steps;        /* > 0: stop the continuation after this many phi
 	                         steps (bounded CPU-baseline sample) */
-	int max_branches;     /* > 0: solve only the first max_branches branches */
+	int max_branches;     /* > 0: solve only max_branches branches: first_branch,
+	                         first_branch + branch_stride, ... (mod num_branches) */
+	int first_branch;
+	int branch_stride;    /* 0 = 1 */
+	int polish_newton;    /* with polish_tol > 0: 1 = polish each root alone by
+	                         FP64 Newton steps z <- z - f / f' on the oracle's
+	                         own f (two evaluations per point); 0 = full Aberth
+	                         sweeps of every column without the early return */
+	int jacobi;           /* 1: every sweep updates a row's roots from the row
+	                         as it stood before the sweep, the roots split over
+	                         the threads (rows one after another: large rows);
+	                         0: the reference's in-place order, rows split over
+	                         the threads.  Both converge to the zeros of f; the
+	                         order of the updates only changes the path. */
 } oracle_params;
 
 typedef struct oracle_info

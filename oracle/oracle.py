@@ -53,6 +53,10 @@ class OracleParams(ctypes.Structure):
         ("exact_binomials", ctypes.c_int),
         ("max_steps", ctypes.c_int),
         ("max_branches", ctypes.c_int),
+        ("first_branch", ctypes.c_int),
+        ("branch_stride", ctypes.c_int),
+        ("polish_newton", ctypes.c_int),
+        ("jacobi", ctypes.c_int),
     ]
 
 
@@ -117,7 +121,8 @@ def build(force: bool = False) -> str:
 
 def build_reference() -> str | None:
     """Compile the reference's own code for the host, if its sources exist here."""
-    ref_dir = os.environ.get("CCF_REFERENCE_DIR", "/root/reference")
+    # the reference checkout sits beside the repository unless CCF_REFERENCE_DIR says otherwise
+    ref_dir = os.environ.get("CCF_REFERENCE_DIR") or os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
     if not os.path.isdir(os.path.join(ref_dir, "include")):
         return None
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFERENCE_DIR={ref_dir}"], check=True)

@@ -31,7 +31,7 @@ def test_library_exports_every_declared_symbol():
     for s in syms:
         assert hasattr(L, s), s
     assert set(syms) == set(_lib.EXPORTED)
-    assert L.ccf_abi_version() == 1
+    assert L.ccf_abi_version() == 2
 
 
 def test_default_params_are_the_reference_defaults():

@@ -92,16 +92,11 @@ def test_golden_fields(path):
     m = O.match_sets(r["ccs"], ref["ccs"], nb)
     assert m["non_finite"] == 0 and m["non_bijective_cols"] == 0
     assert m["max_dist"] <= ROOT_TOL * theta
-    # caustics: inside the convergence disc of the Taylor alpha_smooth the
-    # reference's arithmetic is accurate; outside it carries its own rounding
-    # noise, so those points get the looser bound
+    # caustics: the oracle's lens map at the matched roots, everywhere
     idx, dist = O.match_index(r["ccs"], ref["ccs"], nb)
     w_ref = O.take_matched(ref["caustics"], idx)
-    corner = abs(complex(r["info"]["corner_x1"], r["info"]["corner_x2"]))
-    inside = (np.abs(r["ccs"]) < 0.9 * corner) | (cfg.get("rectangular", 0) == 0)
     dw = np.abs(r["caustics"] - w_ref)
-    assert np.max(dw[inside]) <= ROOT_TOL * theta
-    assert np.max(dw) <= 1e-6 * theta
+    assert np.max(dw) <= ROOT_TOL * theta
     assert np.max(r["errs"]) <= 1e-9
     # the raw reference fixture, on the points where the reference converged
     gi, gd = O.match_index(r["ccs"], g["ccs"], nb)
@@ -172,14 +167,6 @@ def test_star_input_matches_generated_field():
     assert m["max_dist"] <= 1e-12 and m["non_bijective_cols"] == 0
 
 
-def test_precisions_agree():
-    cfg = json.loads(str(np.load(GOLDEN[-1])["params"]))
-    _, a = gpu_run(cfg, "mixed", mu=0)
-    _, b = gpu_run(cfg, "fp64", mu=0)
-    m = O.match_sets(a["ccs"], b["ccs"], cfg["num_branches"])
-    assert m["max_dist"] <= 1e-11 and m["non_bijective_cols"] == 0
-
-
 def test_batch_equals_solo():
     cfgs = [json.loads(str(np.load(p)["params"])) for p in GOLDEN if "exact" not in p]
     solo = [gpu_run(c, "mixed", mu=0)[1] for c in cfgs]
@@ -222,50 +209,3 @@ def test_save_writes_the_reference_layout(tmp_path):
     assert c2.run(-1), c2.last_error()
     m = O.match_sets(c2.results()["ccs"], r["ccs"], 1)
     assert m["max_dist"] <= 1e-12
-
-
-CFG1 = dict(kappa_tot=0.45, kappa_star=0.35, shear=0.35, theta_star=1, mass_function="salpeter", m_lower=0.08,
-            m_upper=1.5, m_solar=4.954984, rectangular=1, approx=1, num_stars=2000, num_phi=2048,
-            num_branches=32, random_seed=1235)
-
-
-def test_full_size_single_field_properties():
-    """2000 Salpeter stars, rectangular field with smooth mass, 2048 phi steps
-    over 32 branches: every point converged and finite, every 1/mu bound below
-    the tolerance, and a sample of columns equal to the polished oracle."""
-    c, r = gpu_run(CFG1, "mixed", mu=0)
-    info = r["info"]
-    assert info["unconverged"] == 0 and info["has_nan"] == 0
-    assert np.isfinite(r["ccs"]).all() and np.isfinite(r["caustics"]).all()
-    # roots a few hundredths of theta_star from a star carry FP64 rounding of
-    # ~1e-9 in f itself (a cancelling m/d^2 ~ 2e3); the 1/mu bound there is
-    # that noise, while a Newton step from the root is ~1e-14
-    assert np.max(r["errs"]) <= 1e-8
-    assert np.quantile(r["errs"], 0.999) <= 1e-9
-    # oracle on a bounded sample: branch 0, centre and the first step each side
-    ref = O.run(num_threads=16, max_branches=1, max_steps=1, polish_tol=1e-13, polish_max_iters=80, **CFG1)
-    nb = CFG1["num_branches"]
-    half = CFG1["num_phi"] // (2 * nb)
-    rows = slice(0, None, nb)
-    cols = [half - 1, half, half + 1]
-    a = r["ccs"][rows][:, cols]
-    b = ref["ccs"][rows][:, cols]
-    m = O.match_sets(a, b, 1)
-    assert m["non_bijective_cols"] == 0 and m["max_dist"] <= ROOT_TOL
-    # caustics of a random sample of points against the oracle's lens map at
-    # the same positions.  The field is large (|corner| ~ 145 theta_star, a
-    # degree-58 Taylor alpha_smooth), which is where a reduced-precision copy
-    # of the polynomial's coefficients would underflow.  Inside 0.9 of the
-    # corner the two agree to rounding; beyond it the reference's polynomial
-    # carries its own rounding noise.
-    sel = np.random.default_rng(3).choice(r["ccs"].size, 4000, replace=False)
-    row, col = np.unravel_index(sel, r["ccs"].shape)
-    phi = np.pi / nb + (row % nb) * 2 * np.pi / nb + (col - half) * 2 * np.pi / CFG1["num_phi"]
-    z = r["ccs"][row, col]
-    o = O.eval_field(z, phi, **CFG1)
-    corner = abs(complex(info["corner_x1"], info["corner_x2"]))
-    inside = np.abs(z) < 0.9 * corner
-    dw = np.abs(r["caustics"][row, col] - o["w"])
-    assert inside.sum() > 1000
-    assert np.max(dw[inside]) <= ROOT_TOL * CFG1["theta_star"]
-    assert np.max(dw) <= 1e-6 * CFG1["theta_star"]
