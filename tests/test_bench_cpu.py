@@ -1,5 +1,6 @@
-"""Host logic of bench.py on the CPU: the FP32 operation count behind the
-roofline, the seeded batch and serving workloads, and the clock record."""
+"""Host logic of bench.py on the CPU: the algorithmic work behind the
+roofline and the executed FP32 operation count beside it, the seeded batch
+and serving workloads, and the clock record."""
 import math
 
 import bench
@@ -8,9 +9,9 @@ HEADLINE_INFO = dict(near_mean=15.68, expansion_order=23, rectangular=1, taylor_
 
 
 def test_smooth_series_charged_to_unfolded_leaves_only():
-    none = bench.tracker_flops_per_eval(dict(HEADLINE_INFO, leaves_folded=0), approx=1)
-    some = bench.tracker_flops_per_eval(dict(HEADLINE_INFO, leaves_folded=1061), approx=1)
-    every = bench.tracker_flops_per_eval(dict(HEADLINE_INFO, leaves_folded=1225), approx=1)
+    none = bench.tracker_ops_per_eval(dict(HEADLINE_INFO, leaves_folded=0), approx=1)
+    some = bench.tracker_ops_per_eval(dict(HEADLINE_INFO, leaves_folded=1061), approx=1)
+    every = bench.tracker_ops_per_eval(dict(HEADLINE_INFO, leaves_folded=1225), approx=1)
     # the base evaluation (near stars, two double-float Horner passes, f' pass, assembly)
     base = 234.0 * 15.68 + 81.0 * (2 * 23 - 3) + 8.0 * 20 + 200.0
     assert math.isclose(every, base)
@@ -20,10 +21,22 @@ def test_smooth_series_charged_to_unfolded_leaves_only():
 
 
 def test_no_series_without_the_rectangular_taylor_form():
-    disc = bench.tracker_flops_per_eval(dict(HEADLINE_INFO, rectangular=0, leaves_folded=0), approx=1)
-    exact = bench.tracker_flops_per_eval(dict(HEADLINE_INFO, leaves_folded=0), approx=0)
+    disc = bench.tracker_ops_per_eval(dict(HEADLINE_INFO, rectangular=0, leaves_folded=0), approx=1)
+    exact = bench.tracker_ops_per_eval(dict(HEADLINE_INFO, leaves_folded=0), approx=0)
     assert math.isclose(disc, exact)
-    assert disc < bench.tracker_flops_per_eval(dict(HEADLINE_INFO, leaves_folded=0), approx=1)
+    assert disc < bench.tracker_ops_per_eval(dict(HEADLINE_INFO, leaves_folded=0), approx=1)
+
+
+def test_algorithmic_work_of_the_headline_field():
+    # 40 per near star, 16 per expansion order, 12 per Taylor term on the unfolded share
+    info = dict(HEADLINE_INFO, leaves_folded=1061)
+    w = bench.algorithmic_flops_per_eval(info, approx=1)
+    assert math.isclose(w, 40 * 15.68 + 16 * 23 + 12 * 56 * (1225 - 1061) / 1225)
+    # the continuation's work adds 10 per reciprocal-sum term outside the initial solve
+    full = dict(info, root_updates=1000, root_updates_init=400, sum_terms=5000, sum_terms_init=2000)
+    assert math.isclose(bench.continuation_algorithmic_flops(full, 1), 10 * 3000 + w * 600)
+    # the double-float emulation executes several FP32 operations per algorithmic flop
+    assert bench.tracker_ops_per_eval(info, 1) / w > 5
 
 
 def test_batch_fields_are_seeded_and_valid():
