@@ -56,7 +56,11 @@ class CcfParams(ctypes.Structure):
         ("device", ctypes.c_int),
         ("continuation", ctypes.c_int),
         ("solved_centres", ctypes.c_int),
-        ("reserved", ctypes.c_int * 6),
+        ("expansion_order", ctypes.c_int),
+        ("leaf_max_stars", ctypes.c_int),
+        ("init_cluster", ctypes.c_int),
+        ("autotune", ctypes.c_int),
+        ("reserved", ctypes.c_int * 2),
     ]
 
 
@@ -117,6 +121,8 @@ class CcfInfo(ctypes.Structure):
         ("unconverged_unpolished", ctypes.c_longlong),
         ("points_polished", ctypes.c_longlong),
         ("points_above_target", ctypes.c_longlong),
+        ("init_cluster", ctypes.c_int),
+        ("leaf_max_stars", ctypes.c_int),
         ("points_at_fp64_floor", ctypes.c_longlong),
     ]
 
@@ -132,7 +138,7 @@ EXPORTED = [
     "ccf_continue_branch_noalloc", "ccf_estimate_device_bytes", "ccf_batch_submit", "ccf_batch_poll",
     "ccf_batch_wait", "ccf_batch_destroy", "ccf_server_create", "ccf_server_submit", "ccf_server_wait",
     "ccf_server_request_info", "ccf_server_handle", "ccf_server_release", "ccf_server_get_stats",
-    "ccf_server_destroy", "ccf_host_alloc", "ccf_host_free",
+    "ccf_server_destroy", "ccf_host_alloc", "ccf_host_free", "ccf_fmm_error", "ccf_autotune",
 ]
 
 REQUEST_QUEUED, REQUEST_RUNNING, REQUEST_DONE, REQUEST_FAILED, REQUEST_REJECTED = range(5)
@@ -223,6 +229,8 @@ def load(path: str | None = None):
         L.ccf_run_batch.argtypes = [ctypes.POINTER(H), ctypes.c_int, ctypes.c_int]
         L.ccf_write_star_file.argtypes = [H, ctypes.c_char_p]
         L.ccf_eval_points.argtypes = [H, ctypes.c_int, dp, dp, dp, dp, dp, dp, dp]
+        L.ccf_fmm_error.argtypes = [H, dp]
+        L.ccf_autotune.argtypes = [H, ctypes.c_int, ctypes.c_int, PP, dp]
         vp = ctypes.c_void_p
         L.ccf_continue_branch_noalloc.argtypes = [H, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp]
         ull = ctypes.c_ulonglong

@@ -69,6 +69,10 @@ class CCF:
         self.device = 0
         self.continuation = "track"
         self.solved_centres = 0
+        self.expansion_order = 0
+        self.leaf_max_stars = 0
+        self.init_cluster = 0
+        self.autotune = 0
         self._stars_keep = None
         self.last_status = 0
         for k, v in kw.items():
@@ -106,6 +110,10 @@ class CCF:
         p.device = int(self.device)
         p.continuation = _continuation_code(self.continuation)
         p.solved_centres = int(self.solved_centres)
+        p.expansion_order = int(self.expansion_order)
+        p.leaf_max_stars = int(self.leaf_max_stars)
+        p.init_cluster = int(self.init_cluster)
+        p.autotune = int(self.autotune)
         return p
 
     def _push(self):
@@ -130,6 +138,31 @@ class CCF:
 
     def last_error(self) -> str:
         return self._L.ccf_last_error(self._h).decode()
+
+    def fmm_error(self) -> float:
+        """Largest far-field error of the last run's field against the direct
+        sum over every star, at one point per leaf (ccf_fmm_error)."""
+        out = ctypes.c_double()
+        rc = self._L.ccf_fmm_error(self._h, ctypes.byref(out))
+        if rc != 0:
+            raise CCFError(rc, self.last_error())
+        return float(out.value)
+
+    def tune(self, fmm: bool = False, verbose: int = 0) -> dict:
+        """Run the autotuner (ccf_autotune) on this field and adopt the
+        settings it finds; returns them with the tuned field's device time.
+        The field must be run again for results."""
+        self._push()
+        best = _lib.CcfParams()
+        secs = ctypes.c_double()
+        rc = self._L.ccf_autotune(self._h, 1 if fmm else 0, int(verbose), ctypes.byref(best), ctypes.byref(secs))
+        if rc != 0:
+            raise CCFError(rc, self.last_error())
+        out = {k: int(getattr(best, k)) for k in ("init_cluster", "solved_centres", "leaf_max_stars", "expansion_order")}
+        for k, v in out.items():
+            setattr(self, k, v)
+        out["seconds"] = float(secs.value)
+        return out
 
     def estimate_device_bytes(self) -> int:
         """Device memory a run with the current parameters holds (upper estimate)."""
@@ -327,6 +360,7 @@ def _bare(**kw) -> CCF:
         "mixed", 0, 300, 60, 0, 0
     c.continuation = "track"
     c.solved_centres = 0
+    c.expansion_order = c.leaf_max_stars = c.init_cluster = c.autotune = 0
     c._stars_keep = None
     c.last_status = 0
     for k, v in kw.items():

@@ -17,6 +17,7 @@ struct ccf_handle
 	std::string last_error;
 };
 
+bool ccf_internal_autotune_apply(ccf_handle* h);   /* autotune.cpp */
 ccf::Field* ccf_internal_field(ccf_handle* h) { return &h->field; }
 ccf::Engine* ccf_internal_engine(ccf_handle* h) { return &h->engine; }
 void ccf_internal_set_error(ccf_handle* h, const std::string& msg) { h->last_error = msg; }
@@ -136,6 +137,8 @@ ccf_status ccf_run(ccf_handle* h, int verbose)
 {
 	if (!h) return CCF_ERR_INVALID_ARGUMENT;
 	h->last_error.clear();
+	if (h->field.params.autotune > 0 && !ccf_internal_autotune_apply(h))
+		return fail(h, CCF_ERR_CUDA, "Error. The autotuner could not run the field: " + h->engine.error);
 	std::vector<ccf::Field*> fs{&h->field};
 	ccf_status rc = h->engine.run(fs, verbose);
 	if (rc != CCF_OK) h->last_error = h->engine.error;
@@ -290,6 +293,23 @@ ccf_status ccf_eval_points(ccf_handle* h, int n, const double* z, const double* 
 	if (e == cudaSuccess && mu_length) e = cudaMemcpyAsync(mu_length, dm.ptr, n * sizeof(double), cudaMemcpyDeviceToHost, s);
 	if (e == cudaSuccess) e = cudaStreamSynchronize(s);
 	if (e != cudaSuccess) return fail(h, CCF_ERR_CUDA, std::string("CUDA error in ccf_eval_points: ") + cudaGetErrorString(e));
+	return CCF_OK;
+}
+
+ccf_status ccf_fmm_error(ccf_handle* h, double* max_error)
+{
+	if (!h || !max_error) return CCF_ERR_INVALID_ARGUMENT;
+	if (!h->field.ran) return fail(h, CCF_ERR_NOT_RUN, "Error. No results: run() has not completed.");
+	cudaStream_t s = h->engine.stream;
+	ccf::DBuf<unsigned long long> out;
+	if (out.ensure(1)) return fail(h, CCF_ERR_OUT_OF_MEMORY, "Error. cudaMalloc failed in ccf_fmm_error");
+	unsigned long long bits = 0;
+	cudaError_t e = cudaMemsetAsync(out.ptr, 0, sizeof(unsigned long long), s);
+	if (e == cudaSuccess) e = ccf::launch_fmm_error(s, h->field.view_dev.ptr, h->field.num_leaves, out.ptr);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(&bits, out.ptr, sizeof(bits), cudaMemcpyDeviceToHost, s);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+	if (e != cudaSuccess) return fail(h, CCF_ERR_CUDA, std::string("CUDA error in ccf_fmm_error: ") + cudaGetErrorString(e));
+	std::memcpy(max_error, &bits, sizeof(double));
 	return CCF_OK;
 }
 

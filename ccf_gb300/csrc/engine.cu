@@ -360,17 +360,20 @@ ccf_status Engine::build_tree(Field& f)
 	f.level_count.assign(1, 1);
 	launch_tree_root(s, f.tree_dev(), rhl, N);
 	CCF_TRY(cudaMemsetAsync(f.level_out.ptr, 0, 4 * sizeof(int), s), "memset");
+	/* a node splits while its stars and its neighbours' exceed the leaf limit
+	   (the reference's 32 unless leaf_max_stars lowers it) */
+	const int limit = f.params.leaf_max_stars > 0 ? std::min(f.params.leaf_max_stars, MAX_NEAR) : MAX_NEAR;
 	int L = 0;
 	while (true)
 	{
 		int start = f.level_start[L], count = f.level_count[L];
 		CCF_TRY(cudaMemsetAsync(f.level_out.ptr, 0, 2 * sizeof(int), s), "memset");
-		launch_tree_flag(s, f.tree_dev(), start, count, f.level_out.ptr);
+		launch_tree_flag(s, f.tree_dev(), start, count, limit, f.level_out.ptr);
 		int hv[3];
 		CCF_TRY(cudaMemcpyAsync(hv, f.level_out.ptr, 3 * sizeof(int), cudaMemcpyDeviceToHost, s), "tree level");
 		CCF_TRY(cudaStreamSynchronize(s), "get_node_star_info");
 		if (hv[2]) { error = "Error. Tree neighbour list overflow."; return CCF_ERR_NUMERIC; }
-		if (hv[0] <= MAX_NEAR) break;
+		if (hv[0] <= limit) break;
 		int nflag = hv[1];
 		int child_start = start + count;
 		int need = child_start + 4 * nflag;
@@ -387,6 +390,7 @@ ccf_status Engine::build_tree(Field& f)
 		if (L > 40) { error = "Error. Tree deeper than 40 levels."; return CCF_ERR_NUMERIC; }
 	}
 	f.num_nodes = f.level_start[L] + f.level_count[L];
+	f.info.leaf_max_stars = limit;
 	return CCF_OK;
 }
 
@@ -399,6 +403,7 @@ ccf_status Engine::build_fmm(Field& f)
 	const double rhl = f.info.root_half_length;
 	/* include/ccf.cuh:840-852 */
 	int P = (int)std::ceil(2 * std::log2(d.theta) + levels - std::log2(rhl) - std::log2(d.alpha_error));
+	if (p.expansion_order > 0) P = p.expansion_order;   /* an explicit order (validated in [3, MAX_ORDER]) */
 	if (P < 3) { error = "Error. Expansion order needs to be >= 3"; return CCF_ERR_INVALID_ARGUMENT; }
 	if (P > MAX_ORDER) { error = "Error. Maximum allowed expansion order is " + std::to_string(MAX_ORDER); return CCF_ERR_INVALID_ARGUMENT; }
 	std::vector<double> B = binomial_table(2 * P, !p.exact_binomials);
@@ -826,6 +831,8 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		while (cl < 16 && (long long)rows * cl * 2 <= slots && minR / (cl * 2) >= 256) cl *= 2;
 		return cl;
 	};
+	/* the initial solve's CTAs per row: as given, else as many as fill the GPU once */
+	const int init_cluster = fields[0]->params.init_cluster;
 	SolveArgs A;
 	std::memset(&A, 0, sizeof(A));
 	A.fields = P.views.ptr;
@@ -837,7 +844,8 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 	if (verbose >= 1) std::cout << "Finding initial roots...\n";
 	A.rows = P.rows_init.ptr;
 	A.num_rows = (int)ri.size();
-	A.cluster = pick_cluster(A.num_rows);
+	A.cluster = init_cluster > 0 ? init_cluster : pick_cluster(A.num_rows);
+	for (Field* f : fields) f->info.init_cluster = A.cluster;
 	A.master = P.master_init.ptr;
 	A.snap32 = mixed ? P.snap32_init.ptr : nullptr;
 	A.snap64 = mixed ? nullptr : P.snap64_init.ptr;

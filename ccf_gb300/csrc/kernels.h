@@ -236,7 +236,7 @@ void launch_star_hilo(cudaStream_t s, int n, const double2* pos, float4* out, co
 
 /* tree.cu */
 void launch_tree_root(cudaStream_t s, const TreeDev& T, double half, int nstars);
-void launch_tree_flag(cudaStream_t s, const TreeDev& T, int start, int count, int* out);
+void launch_tree_flag(cudaStream_t s, const TreeDev& T, int start, int count, int limit, int* out);
 void launch_scan(cudaStream_t s, const int* in, int* out, int n);
 void launch_tree_children(cudaStream_t s, const TreeDev& T, int start, int count, int child_start);
 void launch_tree_partition(cudaStream_t s, const TreeDev& T, int start, int count, double2* pos, double* mass,
@@ -270,6 +270,10 @@ cudaError_t launch_collect_rerun(cudaStream_t s, const TrackArgs& a, RowDesc* re
 cudaError_t launch_clear_tables(cudaStream_t s, const TrackArgs& a);
 cudaError_t launch_eval_points(cudaStream_t s, const FieldView* F_dev, int npts, const double2* z, const double* phi,
 	double2* f, double2* df, double2* w, double* err, double* mu);
+
+/* fmm_check.cu: largest far-field error over one point per leaf (double bits
+   into *out, which must be zero) */
+cudaError_t launch_fmm_error(cudaStream_t s, const FieldView* F_dev, int num_leaves, unsigned long long* out);
 
 /* polish.cu: two launches (scan, list) on s; max_points = the largest field's
    point count (or box); list_count must be zero when they start */

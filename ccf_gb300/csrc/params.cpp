@@ -3,6 +3,7 @@ params.cpp -- host-side parameter checks, derived parameters, smooth-mass
 polynomials, binomial tables and the reference's file formats.
 ******************************************************************************/
 #include "params.h"
+#include "common.cuh"
 #include "mass.h"
 
 #include <algorithm>
@@ -86,6 +87,27 @@ bool check_params(const ccf_params& p, bool star_input, std::string& msg)
 	if (p.solved_centres < 0 || (p.solved_centres > 0 && (p.num_branches <= 0 || p.num_branches % p.solved_centres != 0)))
 	{
 		msg = "Error. solved_centres must be 0 or a divisor of num_branches.";
+		return false;
+	}
+	if (p.expansion_order != 0 && (p.expansion_order < 3 || p.expansion_order > MAX_ORDER))
+	{
+		msg = "Error. expansion_order must be 0 (the reference's formula) or in [3, " + std::to_string(MAX_ORDER) + "].";
+		return false;
+	}
+	if (p.leaf_max_stars != 0 && (p.leaf_max_stars < 4 || p.leaf_max_stars > MAX_NEAR))
+	{
+		msg = "Error. leaf_max_stars must be 0 (the reference's 32) or in [4, " + std::to_string(MAX_NEAR) + "].";
+		return false;
+	}
+	if (p.init_cluster != 0 && p.init_cluster != 1 && p.init_cluster != 2 && p.init_cluster != 4 && p.init_cluster != 8 &&
+		p.init_cluster != 16)
+	{
+		msg = "Error. init_cluster must be 0 (automatic), 1, 2, 4, 8 or 16.";
+		return false;
+	}
+	if (p.autotune < 0 || p.autotune > 2)
+	{
+		msg = "Error. autotune must be 0, 1 or 2.";
 		return false;
 	}
 	return true;

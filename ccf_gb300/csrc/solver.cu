@@ -1072,7 +1072,7 @@ cudaError_t launch_phase_table(cudaStream_t s, int nb, int nphi, PhaseEntry* out
    warp stays in the loop to the end: the evaluation off the root box and
    the direct epilogue are warp-wide calls. */
 template <bool MIXED>
-__global__ void __launch_bounds__(TNT, 4) track_kernel(const TrackArgs T)
+__global__ void __launch_bounds__(TNT, 3) track_kernel(const TrackArgs T)
 {
 	__shared__ FieldView sF[TNT / 32];
 	__shared__ FieldOut sO[TNT / 32];

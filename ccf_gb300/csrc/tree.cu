@@ -2,7 +2,8 @@
 tree.cu -- level-by-level quadtree build on the device.
 
 Same tree as the reference (include/ccf.cuh:781-829, include/tree_node.cuh):
-a node is split when its own stars plus its neighbours' exceed 32; children
+a node is split when its own stars plus its neighbours' exceed 32 (the
+reference's rule; ccf_params.leaf_max_stars may lower the limit); children
 are the four quadrants in the order (+,+), (-,+), (-,-), (+,-); neighbour,
 same-level interaction (M2L) and coarser-leaf interaction (P2L) lists follow
 the reference's distance rules.  Unlike the reference, the build is
@@ -18,7 +19,7 @@ namespace ccf
 
 /* per-level split flags, and the level's max neighbourhood count and number
    of split nodes (tree_node.cuh:321-345) */
-__global__ void tree_flag_kernel(TreeDev T, int start, int count, int* out)
+__global__ void tree_flag_kernel(TreeDev T, int start, int count, int limit, int* out)
 {
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	int ns = 0, flag = 0;
@@ -28,7 +29,7 @@ __global__ void tree_flag_kernel(TreeDev T, int start, int count, int* out)
 		ns = T.star_count[n];
 		int k = T.nbr_count[n];
 		for (int j = 0; j < k; j++) ns += T.star_count[T.nbr[n * MAX_NBR + j]];
-		flag = ns > MAX_NEAR;
+		flag = ns > limit;
 		T.flag[n] = flag;
 	}
 	/* warp-aggregated, order-independent integer atomics */
@@ -271,9 +272,9 @@ void launch_tree_root(cudaStream_t s, const TreeDev& T, double half, int nstars)
 {
 	tree_root_kernel<<<1, 1, 0, s>>>(T, half, nstars);
 }
-void launch_tree_flag(cudaStream_t s, const TreeDev& T, int start, int count, int* out)
+void launch_tree_flag(cudaStream_t s, const TreeDev& T, int start, int count, int limit, int* out)
 {
-	tree_flag_kernel<<<(count + 255) / 256, 256, 0, s>>>(T, start, count, out);
+	tree_flag_kernel<<<(count + 255) / 256, 256, 0, s>>>(T, start, count, limit, out);
 }
 void launch_scan(cudaStream_t s, const int* in, int* out, int n)
 {

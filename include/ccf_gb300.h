@@ -110,7 +110,23 @@ typedef struct ccf_params
 	int solved_centres;          /* tracker: branch centres solved by the initial Aberth solve,
 	                                a divisor of num_branches (the others are reached by
 	                                tracking); 0 (default): as few as fill the GPU */
-	int reserved[6];
+	int expansion_order;         /* FMM expansion order P: 0 (default) = the reference's formula
+	                                (include/ccf.cuh:840-852); 3 .. 31 = this order.  Another
+	                                order than the reference's changes the far field within its
+	                                error target (1e-7 theta_star, include/ccf.cuh:439) and the
+	                                roots with it */
+	int leaf_max_stars;          /* tree split rule: a node is split while its stars and its
+	                                neighbours' exceed this; 0 (default) = 32, the reference's
+	                                (include/tree_node.cuh:14, :321-345); 4 .. 32 (a smaller
+	                                leaf makes the near sums shorter and the tree deeper; it
+	                                changes the far field as expansion_order does) */
+	int init_cluster;            /* CTAs per branch-centre row of the initial Aberth solve:
+	                                0 (default) = as many as fill the GPU once; 1, 2, 4, 8, 16 */
+	int autotune;                /* 1: ccf_run applies the settings ccf_autotune found for fields
+	                                of this shape (init_cluster, solved_centres), tuning on the
+	                                first run of a shape; 2: also expansion_order and
+	                                leaf_max_stars.  0 (default): the settings as given */
+	int reserved[2];
 } ccf_params;
 
 /* Derived parameters, statistics and timings of a run.  Names follow the keys
@@ -187,6 +203,8 @@ typedef struct ccf_info
 	long long points_polished;         /* points the polish worked on */
 	long long points_above_target;     /* polished points whose FP64 1/mu error stays above
 	                                      1e-9 although |f| is above the FP64 floor (below) */
+	int init_cluster;                  /* CTAs per row of the initial Aberth solve */
+	int leaf_max_stars;                /* the tree's leaf limit (32: the reference's rule) */
 	long long points_at_fp64_floor;    /* polished points whose 1/mu error stays above 1e-9
 	                                      because |f| is within four times |f'| times half the
 	                                      FP64 spacing of the root: no FP64 root does better (the
@@ -305,6 +323,28 @@ ccf_status ccf_eval_points(ccf_handle* h, int n, const double* z, const double* 
    serialised by the caller. */
 ccf_status ccf_continue_branch_noalloc(ccf_handle* h, int branch, int side, int num_steps, const double* start_roots,
 	double* ccs, double* errs, double* caustics, void* stream);
+
+/* The largest far-field error of the field built by the last ccf_run: at
+   one point in every leaf, the deflection of the stars from the leaf's near
+   sum and local expansion against the direct sum over every star
+   (include/alpha_star.cuh:18-115 over all stars).  The reference chooses its
+   expansion order so that this stays below alpha_error = 1e-7 theta_star
+   (include/ccf.cuh:439, :840-852).  No reference counterpart. */
+ccf_status ccf_fmm_error(ccf_handle* h, double* max_error);
+
+/* Autotuner: times candidate solver settings on h's field -- init_cluster,
+   solved_centres and, with fmm = 1, leaf_max_stars and expansion_order -- and
+   returns in *best h's parameters with the fastest settings whose runs are
+   as good as the defaults' (no non-finite 1/mu error, no more unconverged
+   points or points above the 1/mu target; for the FMM settings a far-field
+   error within alpha_error or the default's own).  The result is cached per
+   field shape (GPU, precision, continuation, geometry, num_branches, buckets
+   of num_stars and phi steps) in memory and in $CCF_GB300_AUTOTUNE_CACHE
+   (else ~/.cache/ccf_gb300/autotune.txt).  h keeps its parameters; its
+   results are those of the last trial and must be rerun.  best_seconds (may
+   be NULL) receives the tuned field's device time.  No reference counterpart
+   (the reference fixes its launch shapes, leaf size and order). */
+ccf_status ccf_autotune(ccf_handle* h, int fmm, int verbose, ccf_params* best, double* best_seconds);
 
 /* Device memory a run with parameters p will hold (stars, tree, FMM and leaf
    records, solver rows, outputs), an upper estimate used for admission.  No

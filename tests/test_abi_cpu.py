@@ -167,3 +167,20 @@ def test_pinned_host_memory_needs_a_device():
     from ccf_gb300 import CCFError, pinned_empty
     with pytest.raises(CCFError):
         pinned_empty((4, 4))
+
+
+@pytest.mark.parametrize("knob,good,bad,msg", [
+    ("expansion_order", (0, 3, 20, 31), (1, 2, 32), "expansion_order must be 0"),
+    ("leaf_max_stars", (0, 4, 16, 32), (1, 3, 33), "leaf_max_stars must be 0"),
+    ("init_cluster", (0, 1, 2, 4, 8, 16), (3, 5, 32, -1), "init_cluster must be 0"),
+    ("autotune", (0, 1, 2), (3, -1), "autotune must be 0, 1 or 2"),
+])
+def test_solver_and_fmm_settings_are_checked(knob, good, bad, msg):
+    """Settings beside the reference's parameters: 0 keeps the reference's
+    choice (its expansion-order formula, its 32-star leaves) or the
+    library's; other values are range-checked on the host."""
+    for v in good:
+        assert derive_params(**{knob: v})["rc"] == 0, (knob, v)
+    for v in bad:
+        d = derive_params(**{knob: v})
+        assert d["rc"] != 0 and msg in d["error"], (knob, v, d["error"])
