@@ -18,6 +18,7 @@ The engine never resets the device and reuses its buffers across runs.
 #include "engine.h"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -26,6 +27,7 @@ The engine never resets the device and reuses its buffers across runs.
 #include <map>
 #include <mutex>
 #include <numeric>
+#include <thread>
 
 namespace ccf
 {
@@ -119,6 +121,7 @@ Engine::Engine() {}
 
 Engine::~Engine()
 {
+	for (cudaEvent_t e : setup_events) cudaEventDestroy(e);
 	if (stream)
 	{
 		cudaStreamSynchronize(stream);   /* its pool buffers go back to the cache after this */
@@ -1009,6 +1012,81 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 	return status;
 }
 
+/* Star field, tree, FMM and leaf records of every field of a run.  One
+   field's setup is a chain of small launches with a few host round trips
+   (the star statistics, every tree level), so a batch sets its fields up on
+   SETUP_THREADS host threads, each with a CUDA stream of its own: one
+   field's round trips overlap the others' device work.  The solver's stream
+   waits for every setup stream, and the setup streams for the solver's
+   previous work on the same fields. */
+constexpr int SETUP_THREADS = 8;
+constexpr int SETUP_PARALLEL_MIN = 4;
+
+ccf_status Engine::prepare_fields(std::vector<Field*>& fields, int verbose)
+{
+	const int nf = (int)fields.size();
+	const int T = nf >= SETUP_PARALLEL_MIN ? std::min(SETUP_THREADS, nf) : 1;
+	if (T == 1)
+	{
+		for (Field* f : fields)
+		{
+			ccf_status rc = prepare_field(*f, verbose);
+			if (rc != CCF_OK)
+			{
+				f->error = error;
+				return rc;
+			}
+		}
+		return CCF_OK;
+	}
+	while ((int)setup_workers.size() < T)
+	{
+		auto w = std::make_unique<Engine>();
+		if (!w->ensure_device(device))
+		{
+			error = w->error;
+			return CCF_ERR_CUDA;
+		}
+		cudaEvent_t e;
+		CCF_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+		setup_events.push_back(e);
+		setup_workers.push_back(std::move(w));
+	}
+	/* the setup streams start after the solver's previous work */
+	cudaEvent_t start = setup_events[0];
+	CCF_TRY(cudaEventRecord(start, stream), "event");
+	for (int t = 0; t < T; t++) CCF_TRY(cudaStreamWaitEvent(setup_workers[t]->stream, start, 0), "event");
+	std::atomic<int> next{0};
+	std::vector<ccf_status> st(nf, CCF_OK);
+	std::vector<std::thread> threads;
+	for (int t = 0; t < T; t++)
+	{
+		threads.emplace_back([&, t] {
+			Engine& w = *setup_workers[t];
+			cudaSetDevice(device);
+			for (int i; (i = next++) < nf;)
+			{
+				st[i] = w.prepare_field(*fields[i], verbose);
+				if (st[i] != CCF_OK) fields[i]->error = w.error;
+			}
+		});
+	}
+	for (auto& th : threads) th.join();
+	/* the solver's stream waits for every setup stream */
+	for (int t = 0; t < T; t++)
+	{
+		CCF_TRY(cudaEventRecord(setup_events[t], setup_workers[t]->stream), "event");
+		CCF_TRY(cudaStreamWaitEvent(stream, setup_events[t], 0), "event");
+	}
+	for (int i = 0; i < nf; i++)
+		if (st[i] != CCF_OK)
+		{
+			error = fields[i]->error;
+			return st[i];
+		}
+	return CCF_OK;
+}
+
 ccf_status Engine::run(std::vector<Field*>& fields, int verbose)
 {
 	error.clear();
@@ -1018,13 +1096,8 @@ ccf_status Engine::run(std::vector<Field*>& fields, int verbose)
 	{
 		f->ran = false;
 		f->error.clear();
-		ccf_status rc = prepare_field(*f, verbose);
-		if (rc != CCF_OK)
-		{
-			f->error = error;
-			return rc;
-		}
 	}
+	if (ccf_status rc = prepare_fields(fields, verbose); rc != CCF_OK) return rc;
 	ccf_status rc = solve(fields, verbose);
 	if (rc != CCF_OK)
 	{

@@ -188,6 +188,7 @@ public:
 	std::string error;
 
 private:
+	ccf_status prepare_fields(std::vector<Field*>& fields, int verbose);
 	ccf_status prepare_field(Field& f, int verbose);
 	ccf_status build_tree(Field& f);
 	ccf_status build_fmm(Field& f);
@@ -200,6 +201,9 @@ public:
 private:
 
 	SolverPools pools;
+	/* batch setup: engines (their streams) of the setup threads, and events */
+	std::vector<std::unique_ptr<Engine>> setup_workers;
+	std::vector<cudaEvent_t> setup_events;
 	bool initialized = false;
 	int slots_per_sm = 1;
 };
