@@ -219,13 +219,13 @@ class ClockSampler:
 
 # DRAM bytes (read + write) of the continuation launch per continuation point,
 # from the ncu capture summarised in
-# profiles/track_kernel_n2000_salpeter_phi512.md: 89.5 MB for the 4056 * 512
+# profiles/track_kernel_n2000_salpeter_phi512.md: 75.2 MB for the 4056 * 512
 # continuation points of that launch (the 40-byte outputs and the column
 # tables; leaf records and stars stay in L2).  It grows with the points written.
-CONT_DRAM_BYTES_PER_POINT = 89.5e6 / (4056 * 512)
+CONT_DRAM_BYTES_PER_POINT = 75.2e6 / (4056 * 512)
 # FP64-pipe activity of the continuation kernel in the same capture
-# (sm__pipe_fp64_cycles_active over elapsed cycles)
-CONT_FP64_PIPE_ACTIVE = 0.352
+# (sm__pipe_fp64_cycles_active over active cycles)
+CONT_FP64_PIPE_ACTIVE = 0.350
 
 
 def hbm_peak_gbs() -> float | None:
