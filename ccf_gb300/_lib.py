@@ -60,7 +60,8 @@ class CcfParams(ctypes.Structure):
         ("leaf_max_stars", ctypes.c_int),
         ("init_cluster", ctypes.c_int),
         ("autotune", ctypes.c_int),
-        ("reserved", ctypes.c_int * 2),
+        ("host_outputs", ctypes.c_int),
+        ("reserved", ctypes.c_int * 1),
     ]
 
 

@@ -73,6 +73,7 @@ class CCF:
         self.leaf_max_stars = 0
         self.init_cluster = 0
         self.autotune = 0
+        self.host_outputs = 0
         self._stars_keep = None
         self.last_status = 0
         for k, v in kw.items():
@@ -114,6 +115,7 @@ class CCF:
         p.leaf_max_stars = int(self.leaf_max_stars)
         p.init_cluster = int(self.init_cluster)
         p.autotune = int(self.autotune)
+        p.host_outputs = int(self.host_outputs)
         return p
 
     def _push(self):
@@ -360,7 +362,7 @@ def _bare(**kw) -> CCF:
         "mixed", 0, 300, 60, 0, 0
     c.continuation = "track"
     c.solved_centres = 0
-    c.expansion_order = c.leaf_max_stars = c.init_cluster = c.autotune = 0
+    c.expansion_order = c.leaf_max_stars = c.init_cluster = c.autotune = c.host_outputs = 0
     c._stars_keep = None
     c.last_status = 0
     for k, v in kw.items():

@@ -191,10 +191,10 @@ ccf_status ccf_get_device_results(ccf_handle* h, const double** ccs, const doubl
 {
 	if (!h) return CCF_ERR_INVALID_ARGUMENT;
 	if (!h->field.ran) return fail(h, CCF_ERR_NOT_RUN, "Error. No results: run() has not completed.");
-	if (ccs) *ccs = (const double*)h->field.ccs.ptr;
-	if (errs) *errs = h->field.errs.ptr;
-	if (caustics) *caustics = h->field.params.write_caustics ? (const double*)h->field.caustics.ptr : nullptr;
-	if (mu_length_scales) *mu_length_scales = h->field.params.write_mu_length_scales ? h->field.mu.ptr : nullptr;
+	if (ccs) *ccs = (const double*)h->field.out_ccs;
+	if (errs) *errs = h->field.out_errs;
+	if (caustics) *caustics = (const double*)h->field.out_caustics;
+	if (mu_length_scales) *mu_length_scales = h->field.out_mu;
 	return CCF_OK;
 }
 

@@ -289,10 +289,38 @@ ccf_status Engine::prepare_field(Field& f, int verbose)
 	/* outputs */
 	const int R = d.num_roots, nb = p.num_branches, cols = p.num_phi / nb + 1;
 	const size_t npts = (size_t)R * nb * cols;
-	CCF_TRY(f.ccs.ensure(npts), "cudaMalloc(ccs)");
-	CCF_TRY(f.errs.ensure(npts), "cudaMalloc(errs)");
-	if (p.write_caustics) CCF_TRY(f.caustics.ensure(npts), "cudaMalloc(caustics)");
-	if (p.write_mu_length_scales) CCF_TRY(f.mu.ensure(npts), "cudaMalloc(mu_length_scales)");
+	if (p.host_outputs)
+	{
+		/* the kernels write the outputs into page-locked host memory: the device
+		   buffers go back to the cache */
+		f.ccs.release();
+		f.errs.release();
+		f.caustics.release();
+		f.mu.release();
+		CCF_TRY(f.h_ccs.ensure(npts * sizeof(double2)), "cudaHostAlloc(ccs)");
+		CCF_TRY(f.h_errs.ensure(npts * sizeof(double)), "cudaHostAlloc(errs)");
+		if (p.write_caustics) CCF_TRY(f.h_caustics.ensure(npts * sizeof(double2)), "cudaHostAlloc(caustics)");
+		if (p.write_mu_length_scales) CCF_TRY(f.h_mu.ensure(npts * sizeof(double)), "cudaHostAlloc(mu_length_scales)");
+		f.out_ccs = (double2*)f.h_ccs.dev;
+		f.out_errs = (double*)f.h_errs.dev;
+		f.out_caustics = p.write_caustics ? (double2*)f.h_caustics.dev : nullptr;
+		f.out_mu = p.write_mu_length_scales ? (double*)f.h_mu.dev : nullptr;
+	}
+	else
+	{
+		f.h_ccs.release();
+		f.h_errs.release();
+		f.h_caustics.release();
+		f.h_mu.release();
+		CCF_TRY(f.ccs.ensure(npts), "cudaMalloc(ccs)");
+		CCF_TRY(f.errs.ensure(npts), "cudaMalloc(errs)");
+		if (p.write_caustics) CCF_TRY(f.caustics.ensure(npts), "cudaMalloc(caustics)");
+		if (p.write_mu_length_scales) CCF_TRY(f.mu.ensure(npts), "cudaMalloc(mu_length_scales)");
+		f.out_ccs = f.ccs.ptr;
+		f.out_errs = f.errs.ptr;
+		f.out_caustics = p.write_caustics ? f.caustics.ptr : nullptr;
+		f.out_mu = p.write_mu_length_scales ? f.mu.ptr : nullptr;
+	}
 	CCF_TRY(f.stats.ensure(STATS_WORDS), "cudaMalloc(stats)");
 	CCF_TRY(cudaMemsetAsync(f.stats.ptr, 0, STATS_WORDS * sizeof(unsigned long long), s), "memset");
 
@@ -734,10 +762,10 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		views[i] = f.view;
 		FieldOut& o = outs[i];
 		std::memset(&o, 0, sizeof(o));
-		o.ccs = f.ccs.ptr;
-		o.caustics = f.params.write_caustics ? f.caustics.ptr : nullptr;
-		o.errs = f.errs.ptr;
-		o.mu = f.params.write_mu_length_scales ? f.mu.ptr : nullptr;
+		o.ccs = f.out_ccs;
+		o.caustics = f.out_caustics;
+		o.errs = f.out_errs;
+		o.mu = f.out_mu;
 		o.nb = nb;
 		o.nphi = f.params.num_phi;
 		o.cols = f.params.num_phi / nb + 1;
@@ -1111,17 +1139,18 @@ ccf_status Engine::copy_results(Field& f, double* ccs, double* caustics, double*
 {
 	if (!f.ran) { error = "Error. No results: run() has not completed."; return CCF_ERR_NOT_RUN; }
 	const size_t npts = (size_t)f.d.num_roots * f.params.num_branches * (f.params.num_phi / f.params.num_branches + 1);
-	if (ccs) CCF_TRY(cudaMemcpy(ccs, f.ccs.ptr, npts * sizeof(double2), cudaMemcpyDeviceToHost), "copy ccs");
-	if (errs) CCF_TRY(cudaMemcpy(errs, f.errs.ptr, npts * sizeof(double), cudaMemcpyDeviceToHost), "copy errs");
+	/* the outputs sit in device memory or (host_outputs) page-locked host memory */
+	if (ccs) CCF_TRY(cudaMemcpy(ccs, f.out_ccs, npts * sizeof(double2), cudaMemcpyDefault), "copy ccs");
+	if (errs) CCF_TRY(cudaMemcpy(errs, f.out_errs, npts * sizeof(double), cudaMemcpyDefault), "copy errs");
 	if (caustics)
 	{
 		if (!f.params.write_caustics) { error = "Error. Caustics were not requested (write_caustics = 0)."; return CCF_ERR_INVALID_ARGUMENT; }
-		CCF_TRY(cudaMemcpy(caustics, f.caustics.ptr, npts * sizeof(double2), cudaMemcpyDeviceToHost), "copy caustics");
+		CCF_TRY(cudaMemcpy(caustics, f.out_caustics, npts * sizeof(double2), cudaMemcpyDefault), "copy caustics");
 	}
 	if (mu)
 	{
 		if (!f.params.write_mu_length_scales) { error = "Error. Length scales were not requested (write_mu_length_scales = 0)."; return CCF_ERR_INVALID_ARGUMENT; }
-		CCF_TRY(cudaMemcpy(mu, f.mu.ptr, npts * sizeof(double), cudaMemcpyDeviceToHost), "copy mu");
+		CCF_TRY(cudaMemcpy(mu, f.out_mu, npts * sizeof(double), cudaMemcpyDefault), "copy mu");
 	}
 	if (stars)
 	{

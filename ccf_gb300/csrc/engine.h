@@ -78,6 +78,44 @@ struct DBuf
 	size_t bytes() const { return cap * sizeof(T); }
 };
 
+/* grow-only page-locked host buffer mapped into the device's address space:
+   kernels write it through dev (the outputs with ccf_params.host_outputs) */
+struct HostBuf
+{
+	void* ptr = nullptr;
+	void* dev = nullptr;
+	size_t cap = 0;
+	HostBuf() = default;
+	HostBuf(const HostBuf&) = delete;
+	HostBuf& operator=(const HostBuf&) = delete;
+	~HostBuf() { release(); }
+	void release()
+	{
+		if (ptr) cudaFreeHost(ptr);
+		ptr = dev = nullptr;
+		cap = 0;
+	}
+	cudaError_t ensure(size_t bytes)
+	{
+		if (ptr && bytes <= cap) return cudaSuccess;
+		release();
+		cudaError_t e = cudaHostAlloc(&ptr, std::max<size_t>(bytes, 1), cudaHostAllocMapped | cudaHostAllocPortable);
+		if (e != cudaSuccess)
+		{
+			ptr = nullptr;
+			return e;
+		}
+		e = cudaHostGetDevicePointer(&dev, ptr, 0);
+		if (e != cudaSuccess)
+		{
+			release();
+			return e;
+		}
+		cap = bytes;
+		return cudaSuccess;
+	}
+};
+
 /* one field: parameters, derived values, device-resident star field, tree,
    FMM, leaf records and outputs */
 struct Field
@@ -135,9 +173,15 @@ struct Field
 	/* phase of every whole phi step (tracker) */
 	DBuf<PhaseEntry> phase;
 
-	/* outputs, file layout */
+	/* outputs, file layout: device buffers, or page-locked host buffers with
+	   host_outputs; out_* point at the ones in use (device addresses) */
 	DBuf<double2> ccs, caustics;
 	DBuf<double> errs, mu;
+	HostBuf h_ccs, h_caustics, h_errs, h_mu;
+	double2* out_ccs = nullptr;
+	double2* out_caustics = nullptr;
+	double* out_errs = nullptr;
+	double* out_mu = nullptr;
 	DBuf<unsigned long long> stats;   /* solver statistics, 16 words (kernels.h, FieldOut::stats) */
 
 	/* timing */

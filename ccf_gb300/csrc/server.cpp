@@ -50,11 +50,14 @@ unsigned long long estimate_bytes(const ccf_params& p, const ccf::Derived& d)
 	/* tracker: column tables (2 R slots of 8 bytes per phi step of every row),
 	   solo-root lists (9 bytes per root of a row), row records and statistics */
 	if (p.continuation == CCF_CONTINUATION_TRACK) b += 2 * nb * (cols / 2) * 2 * R * 8 + 2 * nb * R * 9 + 2 * nb * (40 + 40);
-	/* outputs in the file layout */
+	/* outputs in the file layout (none on the device with host_outputs) */
 	const unsigned long long pts = R * nb * cols;
-	b += pts * (16 + 8);
-	if (p.write_caustics) b += pts * 16;
-	if (p.write_mu_length_scales) b += pts * 8;
+	if (!p.host_outputs)
+	{
+		b += pts * (16 + 8);
+		if (p.write_caustics) b += pts * 16;
+		if (p.write_mu_length_scales) b += pts * 8;
+	}
 	return b + (64ull << 20);
 }
 

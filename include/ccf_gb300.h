@@ -126,7 +126,13 @@ typedef struct ccf_params
 	                                of this shape (init_cluster, solved_centres), tuning on the
 	                                first run of a shape; 2: also expansion_order and
 	                                leaf_max_stars.  0 (default): the settings as given */
-	int reserved[2];
+	int host_outputs;            /* 1: the outputs (roots, caustics, 1/mu errors, length scales)
+	                                are written by the kernels straight into page-locked host
+	                                memory that the library holds, mapped into the GPU's address
+	                                space: they take no device memory and need no copy after the
+	                                run (on GB300 the GPU writes it over NVLink-C2C).  0 (default):
+	                                device memory */
+	int reserved[1];
 } ccf_params;
 
 /* Derived parameters, statistics and timings of a run.  Names follow the keys
@@ -257,7 +263,9 @@ ccf_status ccf_get_results(ccf_handle* h, double* ccs, double* caustics, double*
 	double* mu_length_scales, double* stars);
 
 /* Device pointers of the same arrays (valid until the next run or destroy);
-   a pointer is NULL when that output was not requested. */
+   a pointer is NULL when that output was not requested.  With
+   ccf_params.host_outputs they address page-locked host memory, which the
+   host can read through the same pointers. */
 ccf_status ccf_get_device_results(ccf_handle* h, const double** ccs, const double** caustics,
 	const double** errs, const double** mu_length_scales);
 

@@ -11,6 +11,7 @@ autotuner that picks them.
   FP32 sums: the same zero sets.
 * the autotuner returns valid settings, caches them per field shape, and a
   run with autotune set applies them.
+* host_outputs: the same bits with the outputs in page-locked host memory.
 """
 import os
 
@@ -107,3 +108,26 @@ def test_autotune_caches_and_applies(tmp_path, monkeypatch):
     ref = run(cfg)
     m = O.match_sets(d.results(stars=False)["ccs"], ref.results(stars=False)["ccs"], cfg["num_branches"])
     assert m["non_bijective_cols"] == 0 and m["max_dist"] <= 1e-9, m
+
+
+def test_host_outputs_are_the_same_bits_without_device_output_memory():
+    """host_outputs: the kernels write the outputs into page-locked host
+    memory mapped into the GPU; the results are bit for bit those of device
+    outputs, the admission estimate drops by the outputs' bytes, and the
+    library's output pointers read directly from the host."""
+    import ctypes
+    cfg = dict(CFG1, num_phi=512)
+    a = run(cfg)
+    b = run(cfg, host_outputs=1)
+    ra, rb = a.results(stars=False), b.results(stars=False)
+    for k in ("ccs", "caustics", "errs"):
+        assert np.array_equal(ra[k], rb[k]), k
+    assert b.estimate_device_bytes() < a.estimate_device_bytes()
+    pts = ra["ccs"].size
+    assert a.estimate_device_bytes() - b.estimate_device_bytes() == pts * 40
+    # the output pointers of a host_outputs run address host memory
+    ccs, caus, errs, mu = (ctypes.c_void_p() for _ in range(4))
+    assert b._L.ccf_get_device_results(b._h, ctypes.byref(ccs), ctypes.byref(caus), ctypes.byref(errs),
+                                       ctypes.byref(mu)) == 0
+    host_errs = np.ctypeslib.as_array(ctypes.cast(errs.value, ctypes.POINTER(ctypes.c_double)), shape=(pts,))
+    assert np.array_equal(host_errs.reshape(ra["errs"].shape), ra["errs"])
