@@ -32,9 +32,11 @@ point), forms the largest error of the points that need nothing, and lists
 the flagged ones (warp-aggregated appends); flagged points are consecutive
 phi steps of the same stiff roots, so polishing them where they are found
 would serialise them in a few warps.  polish_list_kernel then gives every
-listed point its own warp: the lanes split the near stars (or, off the root
-box, all stars), and every lane holds the same sums.  A point beyond the
-list's capacity is polished by the scan itself.
+listed point a lane of its own with its leaf's near sums (the FP64 pipe does
+32 points' work per warp instruction); a point off the root box, whose sums
+run over every star, is taken by the whole warp, the lanes splitting the
+stars.  A point beyond the list's capacity is polished by the scan itself,
+one warp per point.
 ******************************************************************************/
 #include "kernels.h"
 
@@ -105,6 +107,24 @@ __device__ void warp_point_sums(const FieldView& F, int leaf, double2 z, NearSum
 	pole = make_double2(v[6], v[7]);
 }
 
+/* the same sums for one lane's own point over its leaf's near stars */
+__device__ void lane_point_sums(const FieldView& F, int leaf, double2 z, NearSums& S, double2& pole)
+{
+	S = zero_sums();
+	double px = 0, py = 0;
+	const int n = F.leaf_near_count[leaf];
+	const NearStar* ns = F.leaf_near + (size_t)leaf * MAX_NEAR;
+	for (int i = 0; i < n; i++)
+	{
+		const NearStar st = ns[i];
+		star_term<true, true>(S, z, st.x, st.y, st.m);
+		const double2 id = cinv(make_double2(z.x - st.x, z.y - st.y));
+		px += id.x;
+		py += id.y;
+	}
+	pole = make_double2(px, py);
+}
+
 /* phase of output column k of branch b: phi0 + sgn 2 pi j / nphi with
    phi0 = pi / nb + 2 pi b / nb, as the reference forms it
    (include/ccf_functions.cuh:338, :344) */
@@ -158,13 +178,19 @@ __device__ double fp64_floor(double2 z, double2 df)
 	return 0.5 * hypot(ux, uy) * hypot(df.x, df.y);
 }
 
-/* Polish the point in output slot idx (warp-wide; every lane passes the same
-   arguments).  e0: its stored 1/mu error (unmarked); listed: the solver left
-   it unconverged. */
+/* Polish the point in output slot idx.  e0: its stored 1/mu error
+   (unmarked); listed: the solver left it unconverged.  WARP: the whole warp
+   works on one point (every lane passes the same arguments; the lanes split
+   the star sums, which off the root box run over every star).  Otherwise each
+   lane polishes a point of its own with its leaf's near sums, 32 points per
+   warp instruction on the FP64 pipe; a lane whose point is (or gets) off the
+   root box sets *off and writes nothing, for the warp to take it. */
+template <bool WARP>
 __device__ __noinline__ PolishOutcome polish_point(const FieldView& F, const FieldOut& O, size_t idx, double e0,
-	bool listed)
+	bool listed, bool* off)
 {
 	const int lane = threadIdx.x & 31;
+	const bool writer = WARP ? lane == 0 : true;
 	const size_t row = idx / (size_t)O.cols;
 	const int k = (int)(idx - row * (size_t)O.cols);
 	const int b = (int)(row % (size_t)O.nb);
@@ -186,7 +212,20 @@ __device__ __noinline__ PolishOutcome polish_point(const FieldView& F, const Fie
 		const int leaf = find_leaf(F, z);
 		NearSums S;
 		double2 pole;
-		warp_point_sums(F, leaf, z, S, pole);
+		if constexpr (WARP) warp_point_sums(F, leaf, z, S, pole);
+		else
+		{
+			if (leaf < 0)
+			{
+				*off = true;
+				PolishOutcome none;
+				none.err = e0;
+				none.conv = false;
+				none.floor = false;
+				return none;
+			}
+			lane_point_sums(F, leaf, z, S, pole);
+		}
 		const PolishEval v = polish_eval(F, leaf, z, cp, sp, S);
 		const double af = hypot(v.f.x, v.f.y);
 		const double err = fmax(fabs(af * (af + 2 * v.a)), fabs(af * (af - 2 * v.a)));
@@ -228,7 +267,7 @@ __device__ __noinline__ PolishOutcome polish_point(const FieldView& F, const Fie
 	out.floor = false;
 	if (!have)
 	{
-		if (lane == 0 && listed) O.errs[idx] = e0;   /* a listed point gets its mark removed */
+		if (writer && listed) O.errs[idx] = e0;   /* a listed point gets its mark removed */
 		out.err = e0;
 		out.conv = false;
 		return out;
@@ -247,7 +286,7 @@ __device__ __noinline__ PolishOutcome polish_point(const FieldView& F, const Fie
 	{
 		/* the root stays: its FP64 1/mu error replaces the bound (the caustic
 		   and length scale of the solver stand) */
-		if (lane == 0) O.errs[idx] = erb;
+		if (writer) O.errs[idx] = erb;
 		out.err = erb;
 	}
 	else if (improve)
@@ -258,7 +297,7 @@ __device__ __noinline__ PolishOutcome polish_point(const FieldView& F, const Fie
 		else if (O.caustics) pr = eval_point<true, false>(F, lb, zb, cp, sp, Sb);
 		else if (O.mu) pr = eval_point<false, true>(F, lb, zb, cp, sp, Sb);
 		else pr = eval_point<false, false>(F, lb, zb, cp, sp, Sb);
-		if (lane == 0)
+		if (writer)
 		{
 			O.ccs[idx] = zb;
 			O.errs[idx] = pr.err;
@@ -270,7 +309,7 @@ __device__ __noinline__ PolishOutcome polish_point(const FieldView& F, const Fie
 	else
 	{
 		/* keep the stored point; a listed point gets its mark removed */
-		if (lane == 0 && listed) O.errs[idx] = e0;
+		if (writer && listed) O.errs[idx] = e0;
 		out.err = e0;
 	}
 	out.floor = afb <= POLISH_FLOOR * fp64_floor(zb, dfb);
@@ -365,7 +404,7 @@ __global__ void __launch_bounds__(256) polish_scan_kernel(const PolishArgs A)
 			const size_t pidx = (size_t)__shfl_sync(full, (unsigned long long)idx, src);
 			const double pe = __shfl_sync(full, e, src);
 			const bool listed = pe < 0;
-			const PolishOutcome o = polish_point(F, O, pidx, listed ? -1 - pe : pe, listed);
+			const PolishOutcome o = polish_point<true>(F, O, pidx, listed ? -1 - pe : pe, listed, nullptr);
 			if (lane == src)
 			{
 				polished++;
@@ -383,26 +422,72 @@ __global__ void __launch_bounds__(256) polish_scan_kernel(const PolishArgs A)
 	polish_stats(O.stats, maxe, nan, polished, unconv, above, at_floor);
 }
 
-/* one warp per listed point */
+/* one lane per listed point (lanes on points off the root box hand them to
+   the whole warp) */
 __global__ void __launch_bounds__(256) polish_list_kernel(const PolishArgs A)
 {
+	const unsigned full = 0xffffffffu;
 	const int lane = threadIdx.x & 31;
 	const unsigned long long n = min(*A.list_count, (unsigned long long)A.list_cap);
-	const unsigned long long nw = (unsigned long long)gridDim.x * (blockDim.x >> 5);
-	for (unsigned long long q = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); q < n; q += nw)
+	const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+	/* warp-uniform trip count: the off-field points are warp-wide calls */
+	for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n;
+		base += stride)
 	{
-		const unsigned long long ent = A.list[q];
-		const int fi = (int)(ent >> LIST_FIELD_SHIFT);
-		const size_t idx = (size_t)(ent & ((1ull << LIST_FIELD_SHIFT) - 1));
-		const FieldView& F = A.fields[fi];
-		const FieldOut& O = A.outs[fi];
-		const double pe = O.errs[idx];
-		const bool listed = pe < 0;
-		const PolishOutcome o = polish_point(F, O, idx, listed ? -1 - pe : pe, listed);
+		const unsigned long long q = base + lane;
+		const bool v = q < n;
+		int fi = 0;
+		size_t idx = 0;
+		double e0 = 0;
+		bool listed = false, off = false;
+		PolishOutcome o;
+		o.err = 0;
+		o.conv = true;
+		o.floor = false;
+		if (v)
+		{
+			const unsigned long long ent = A.list[q];
+			fi = (int)(ent >> LIST_FIELD_SHIFT);
+			idx = (size_t)(ent & ((1ull << LIST_FIELD_SHIFT) - 1));
+			const double pe = A.outs[fi].errs[idx];
+			listed = pe < 0;
+			e0 = listed ? -1 - pe : pe;
+			o = polish_point<false>(A.fields[fi], A.outs[fi], idx, e0, listed, &off);
+		}
+		unsigned m = __ballot_sync(full, v && off);
+		while (m)
+		{
+			const int src = __ffs(m) - 1;
+			m &= m - 1;
+			const int f2 = __shfl_sync(full, fi, src);
+			const size_t i2 = (size_t)__shfl_sync(full, (unsigned long long)idx, src);
+			const double e2 = __shfl_sync(full, e0, src);
+			const bool l2 = __shfl_sync(full, (int)listed, src) != 0;
+			const PolishOutcome ow = polish_point<true>(A.fields[f2], A.outs[f2], i2, e2, l2, nullptr);
+			if (lane == src) o = ow;
+		}
 		const bool fin = isfinite(o.err);
-		const bool high = lane == 0 && !(o.err <= POLISH_ERR);
-		polish_stats(O.stats, lane == 0 && fin ? o.err : 0, lane == 0 && !fin, lane == 0 ? 1 : 0,
-			lane == 0 && listed && !o.conv ? 1 : 0, high && !o.floor ? 1 : 0, high && o.floor ? 1 : 0);
+		const bool high = v && !(o.err <= POLISH_ERR);
+		const double me = v && fin ? o.err : 0;
+		const unsigned long long un = v && listed && !o.conv ? 1 : 0;
+		const unsigned long long ab = high && !o.floor ? 1 : 0, fl = high && o.floor ? 1 : 0;
+		/* the statistics go to each point's field: warp sums when the warp's
+		   points share one field */
+		const int f0 = __shfl_sync(full, fi, 0);
+		if (__all_sync(full, !v || fi == f0))
+		{
+			polish_stats(A.outs[f0].stats, me, v && !fin, v ? 1 : 0, un, ab, fl);
+		}
+		else if (v)
+		{
+			unsigned long long* st = A.outs[fi].stats;
+			atomicMax(&st[STAT_POLISHED_MAX_ERR], (unsigned long long)__double_as_longlong(me));
+			if (!fin) atomicOr(&st[STAT_POLISHED_NAN], 1ull);
+			atomicAdd(&st[STAT_POLISHED], 1ull);
+			if (un) atomicAdd(&st[STAT_POLISHED_UNCONV], un);
+			if (ab) atomicAdd(&st[STAT_POLISHED_ABOVE], ab);
+			if (fl) atomicAdd(&st[STAT_POLISHED_FLOOR], fl);
+		}
 	}
 }
 
@@ -418,7 +503,7 @@ cudaError_t launch_polish(cudaStream_t s, const PolishArgs& a, long long max_poi
 	polish_scan_kernel<<<dim3((unsigned)bx, (unsigned)a.num_fields), 256, 0, s>>>(a);
 	cudaError_t e = cudaGetLastError();
 	if (e != cudaSuccess || a.list_cap <= 0) return e;
-	/* the list: 8 warps per block, 8 blocks per SM, each warp striding */
+	/* the list: one lane per point, 8 blocks of 256 per SM, striding */
 	polish_list_kernel<<<8 * num_sms, 256, 0, s>>>(a);
 	return cudaGetLastError();
 }
