@@ -22,6 +22,7 @@ The engine never resets the device and reuses its buffers across runs.
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <iostream>
 #include <map>
@@ -122,6 +123,12 @@ Engine::Engine() {}
 Engine::~Engine()
 {
 	for (cudaEvent_t e : setup_events) cudaEventDestroy(e);
+	if (chunk.copy)
+	{
+		cudaStreamSynchronize(chunk.copy);
+		cudaStreamDestroy(chunk.copy);
+		for (cudaEvent_t e : {chunk.ready, chunk.copied[0], chunk.copied[1], chunk.done}) cudaEventDestroy(e);
+	}
 	if (stream)
 	{
 		cudaStreamSynchronize(stream);   /* its pool buffers go back to the cache after this */
@@ -291,8 +298,9 @@ ccf_status Engine::prepare_field(Field& f, int verbose)
 	const size_t npts = (size_t)R * nb * cols;
 	if (p.host_outputs)
 	{
-		/* the kernels write the outputs into page-locked host memory: the device
-		   buffers go back to the cache */
+		/* the outputs live in page-locked host memory (written there by the
+		   kernels, or by the chunk copies of solve_chunked): the device buffers
+		   go back to the cache */
 		f.ccs.release();
 		f.errs.release();
 		f.caustics.release();
@@ -669,6 +677,17 @@ static size_t nb_total(const std::vector<Field*>& fields)
 /* largest number of branches per solved centre the engine picks by itself */
 constexpr int MAX_SEG = 16;
 
+int Engine::solved_seg(const Field& f, bool track) const
+{
+	const long long lanes_wanted = 2LL * num_sms * 16 * 32;
+	const int R = f.d.num_roots, nb = f.params.num_branches;
+	if (!track) return 1;
+	if (f.params.solved_centres > 0) return nb / f.params.solved_centres;
+	for (int g = std::min(nb, MAX_SEG); g > 1; g--)
+		if (nb % g == 0 && 2LL * (nb / g) * R >= lanes_wanted) return g;
+	return 1;
+}
+
 ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 {
 	cudaStream_t s = stream;
@@ -697,21 +716,8 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 	   bounds the chain of a root that starts off the root box, which one warp
 	   tracks alone with direct star sums (on the 20000-star field 8 of 128
 	   centres take 0.62 s per field, 2 centres 3.2 s, all 128 1.50 s). */
-	const long long lanes_wanted = 2LL * num_sms * 16 * 32;
 	std::vector<int> seg(nf);
-	for (int i = 0; i < nf; i++)
-	{
-		const int R = fields[i]->d.num_roots, nb = fields[i]->params.num_branches;
-		seg[i] = 1;
-		if (track && fields[i]->params.solved_centres > 0) seg[i] = nb / fields[i]->params.solved_centres;
-		else if (track)
-			for (int g = std::min(nb, MAX_SEG); g > 1; g--)
-				if (nb % g == 0 && 2LL * (nb / g) * R >= lanes_wanted)
-				{
-					seg[i] = g;
-					break;
-				}
-	}
+	for (int i = 0; i < nf; i++) seg[i] = solved_seg(*fields[i], track);
 	/* row offsets */
 	std::vector<long long> init_off(nf), cont_off(nf);
 	long long ninit = 0, ncont = 0;
@@ -772,6 +778,7 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		o.half = f.params.num_phi / (2 * nb);
 		o.step_first = 1;
 		o.step_last = o.half;
+		full_window(o);
 		o.max_iters_init = f.params.max_iters_init;
 		o.max_iters_step = f.params.max_iters_step;
 		o.seg = seg[i];
@@ -983,77 +990,100 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 	CCF_TRY(cudaStreamSynchronize(s), "solver");
 
 	ccf_status status = CCF_OK;
+	/* root seeds, initial solve, continuation (tracker: phase table, item
+	   marking, tracking, row collection, table clearing, re-tracking, row
+	   collection and the full-sum launch for the rows to re-run), FP64 polish */
 	for (int fi = 0; fi < nf; fi++)
 	{
-		Field* f = fields[fi];
-		unsigned long long st[STATS_WORDS];
-		CCF_TRY(cudaMemcpy(st, f->stats.ptr, STATS_WORDS * sizeof(unsigned long long), cudaMemcpyDeviceToHost), "stats");
-		ccf_info& info = f->info;
-		double me;
-		std::memcpy(&me, &st[STAT_POLISHED_MAX_ERR], sizeof(double));
-		info.max_error = me;
-		std::memcpy(&me, &st[0], sizeof(double));
-		info.max_error_unpolished = me;
-		info.has_nan = st[STAT_POLISHED_NAN] ? 1 : 0;
-		info.root_updates = (long long)st[2];
-		info.sum_terms = (long long)st[3];
-		info.unconverged = (long long)st[STAT_POLISHED_UNCONV];
-		info.unconverged_unpolished = (long long)st[4];
-		info.points_polished = (long long)st[STAT_POLISHED];
-		info.points_above_target = (long long)st[STAT_POLISHED_ABOVE];
-		info.points_at_fp64_floor = (long long)st[STAT_POLISHED_FLOOR];
-		info.max_sweeps_init = (int)st[5];
-		info.max_sweeps_step = (int)st[6];
-		info.root_updates_init = (long long)st[7];
-		info.sum_terms_init = (long long)st[8];
-		info.rows_rerun = (long long)st[9];
-		info.step_halvings = (long long)st[10];
-		info.rerun_flags = (long long)st[11];
-		info.rows_retracked = (int)st[12];
-		info.t_stars = ev_ms(f->ev[0], f->ev[1]) * 1e-3;
-		info.t_tree = ev_ms(f->ev[1], f->ev[2]) * 1e-3;
-		info.t_init_roots = ev_ms(f->ev[3], f->ev[4]) * 1e-3;
-		info.t_ccs = ev_ms(f->ev[4], f->ev[6]) * 1e-3;
-		info.t_caustics = ev_ms(f->ev[6], f->ev[5]) * 1e-3;
-		info.t_total = ev_ms(f->ev[0], f->ev[5]) * 1e-3;
-		/* root seeds, initial solve, continuation (tracker: phase table, item
-		   marking, tracking, row collection, table clearing, re-tracking, row
-		   collection and the full-sum launch for the rows to re-run), FP64 polish */
-		info.kernel_launches += track ? 12 : 5;
-		info.centres_solved = f->params.num_branches / seg[fi];
-		if (info.has_nan)
-		{
-			f->error = "Error. Errors in 1/mu contain values which are not positive real numbers.";
-			status = CCF_ERR_NUMERIC;
-		}
-		else
-		{
-			f->ran = true;
-		}
-		if (verbose >= 1)
-		{
-			std::cout << "Done finding critical curve positions. Elapsed time: " << info.t_init_roots + info.t_ccs << " seconds.\n";
-			std::cout << "Maximum error in 1/mu: " << info.max_error << "\n";
-		}
+		ccf_status rc = finish_stats(*fields[fi], seg[fi], track, verbose, track ? 12 : 5);
+		if (rc != CCF_OK) status = rc;
 	}
-	if (status != CCF_OK) error = "Error. Errors in 1/mu contain values which are not positive real numbers.";
+	return status;
+}
+
+/* statistics and timings of a field's run into its info; the field is ran
+   unless a 1/mu error is not finite */
+ccf_status Engine::finish_stats(Field& f, int seg, bool track, int verbose, int launches)
+{
+	(void)track;
+	unsigned long long st[STATS_WORDS];
+	CCF_TRY(cudaMemcpy(st, f.stats.ptr, STATS_WORDS * sizeof(unsigned long long), cudaMemcpyDeviceToHost), "stats");
+	ccf_info& info = f.info;
+	double me;
+	std::memcpy(&me, &st[STAT_POLISHED_MAX_ERR], sizeof(double));
+	info.max_error = me;
+	std::memcpy(&me, &st[0], sizeof(double));
+	info.max_error_unpolished = me;
+	info.has_nan = st[STAT_POLISHED_NAN] ? 1 : 0;
+	info.root_updates = (long long)st[2];
+	info.sum_terms = (long long)st[3];
+	info.unconverged = (long long)st[STAT_POLISHED_UNCONV];
+	info.unconverged_unpolished = (long long)st[4];
+	info.points_polished = (long long)st[STAT_POLISHED];
+	info.points_above_target = (long long)st[STAT_POLISHED_ABOVE];
+	info.points_at_fp64_floor = (long long)st[STAT_POLISHED_FLOOR];
+	info.max_sweeps_init = (int)st[5];
+	info.max_sweeps_step = (int)st[6];
+	info.root_updates_init = (long long)st[7];
+	info.sum_terms_init = (long long)st[8];
+	info.rows_rerun = (long long)st[9];
+	info.step_halvings = (long long)st[10];
+	info.rerun_flags = (long long)st[11];
+	info.rows_retracked = (int)st[12];
+	info.t_stars = ev_ms(f.ev[0], f.ev[1]) * 1e-3;
+	info.t_tree = ev_ms(f.ev[1], f.ev[2]) * 1e-3;
+	info.t_init_roots = ev_ms(f.ev[3], f.ev[4]) * 1e-3;
+	info.t_ccs = ev_ms(f.ev[4], f.ev[6]) * 1e-3;
+	info.t_caustics = ev_ms(f.ev[6], f.ev[5]) * 1e-3;
+	info.t_total = ev_ms(f.ev[0], f.ev[5]) * 1e-3;
+	info.kernel_launches += launches;
+	info.centres_solved = f.params.num_branches / seg;
+	ccf_status status = CCF_OK;
+	if (info.has_nan)
+	{
+		f.error = "Error. Errors in 1/mu contain values which are not positive real numbers.";
+		error = f.error;
+		status = CCF_ERR_NUMERIC;
+	}
+	else
+	{
+		f.ran = true;
+	}
+	if (verbose >= 1)
+	{
+		std::cout << "Done finding critical curve positions. Elapsed time: " << info.t_init_roots + info.t_ccs << " seconds.\n";
+		std::cout << "Maximum error in 1/mu: " << info.max_error << "\n";
+	}
 	return status;
 }
 
 /* Star field, tree, FMM and leaf records of every field of a run.  One
    field's setup is a chain of small launches with a few host round trips
    (the star statistics, every tree level), so a batch sets its fields up on
-   SETUP_THREADS host threads, each with a CUDA stream of its own: one
+   SETUP_THREADS host threads (12: on the 16-core Grace host 8 give 342 ms
+   per 256-field pass, 12 335, 16 333), each with a CUDA stream of its own: one
    field's round trips overlap the others' device work.  The solver's stream
    waits for every setup stream, and the setup streams for the solver's
    previous work on the same fields. */
-constexpr int SETUP_THREADS = 8;
+constexpr int SETUP_THREADS = 12;
 constexpr int SETUP_PARALLEL_MIN = 4;
+
+/* setup threads: SETUP_THREADS, or the CCF_GB300_SETUP_THREADS environment
+   variable (1 .. 64) */
+static int setup_threads()
+{
+	static const int n = [] {
+		const char* e = std::getenv("CCF_GB300_SETUP_THREADS");
+		const int v = e ? std::atoi(e) : 0;
+		return v >= 1 && v <= 64 ? v : SETUP_THREADS;
+	}();
+	return n;
+}
 
 ccf_status Engine::prepare_fields(std::vector<Field*>& fields, int verbose)
 {
 	const int nf = (int)fields.size();
-	const int T = nf >= SETUP_PARALLEL_MIN ? std::min(SETUP_THREADS, nf) : 1;
+	const int T = nf >= SETUP_PARALLEL_MIN ? std::min(setup_threads(), nf) : 1;
 	if (T == 1)
 	{
 		for (Field* f : fields)
@@ -1126,7 +1156,8 @@ ccf_status Engine::run(std::vector<Field*>& fields, int verbose)
 		f->error.clear();
 	}
 	if (ccf_status rc = prepare_fields(fields, verbose); rc != CCF_OK) return rc;
-	ccf_status rc = solve(fields, verbose);
+	ccf_status rc = fields.size() == 1 && fields[0]->params.host_outputs == 2 ? solve_chunked(*fields[0], verbose)
+	                                                                            : solve(fields, verbose);
 	if (rc != CCF_OK)
 	{
 		for (Field* f : fields)

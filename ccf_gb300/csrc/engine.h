@@ -237,6 +237,9 @@ private:
 	ccf_status build_tree(Field& f);
 	ccf_status build_fmm(Field& f);
 	ccf_status solve(std::vector<Field*>& fields, int verbose);
+	ccf_status solve_chunked(Field& f, int verbose);   /* stream.cu */
+	int solved_seg(const Field& f, bool track) const;
+	ccf_status finish_stats(Field& f, int seg, bool track, int verbose, int launches);
 	ccf_status cuda_fail(cudaError_t e, const char* what);
 
 public:
@@ -245,6 +248,19 @@ public:
 private:
 
 	SolverPools pools;
+	/* solve_chunked: the centre columns of the initial solve, two chunk
+	   buffers of output windows, their FieldOut records, a copy stream and
+	   its events */
+	struct ChunkState
+	{
+		DBuf<double2> ctr_ccs, ctr_caus;
+		DBuf<double> ctr_errs, ctr_mu;
+		DBuf<double2> ccs[2], caus[2];
+		DBuf<double> errs[2], mu[2];
+		DBuf<FieldOut> outs;
+		cudaStream_t copy = nullptr;
+		cudaEvent_t ready = nullptr, copied[2] = {nullptr, nullptr}, done = nullptr;
+	} chunk;
 	/* batch setup: engines (their streams) of the setup threads, and events */
 	std::vector<std::unique_ptr<Engine>> setup_workers;
 	std::vector<cudaEvent_t> setup_events;

@@ -80,6 +80,10 @@ struct FieldOut
 	double2* cont_master;
 	float4* cont_snap32;
 	double2* cont_snap64;
+	/* the output window: the arrays hold branches w_b0 .. w_b0 + w_nb - 1
+	   (mod nb) and columns w_k0 .. w_k0 + w_cols - 1 of each, in the file
+	   layout's order; the whole field is (0, nb, 0, cols) */
+	int w_b0, w_nb, w_k0, w_cols;
 	/* statistics */
 	unsigned long long* stats;   /* STATS_WORDS words: [0] max_err bits, [1] nan flag, [2] updates,
 	                                [3] terms, [4] unconverged, [5] max sweeps init, [6] max sweeps
@@ -89,6 +93,25 @@ struct FieldOut
 	                                [12] rows tracked again with fine sub-steps; [16] .. [20] the
 	                                FP64 polish (STAT_POLISHED_*) */
 };
+
+/* slot of root a, branch b, column k in the window's arrays; NO_OUT when
+   the window does not hold that column */
+constexpr size_t NO_OUT = ~(size_t)0;
+CCF_HD size_t out_slot(const FieldOut& O, int a, int b, int k)
+{
+	int bi = b - O.w_b0;
+	if (bi < 0) bi += O.nb;
+	const int ki = k - O.w_k0;
+	if (bi >= O.w_nb || ki < 0 || ki >= O.w_cols) return NO_OUT;
+	return ((size_t)a * O.w_nb + bi) * O.w_cols + ki;
+}
+CCF_HD void full_window(FieldOut& O)
+{
+	O.w_b0 = 0;
+	O.w_nb = O.nb;
+	O.w_k0 = 0;
+	O.w_cols = O.cols;
+}
 
 /* statistics words of a field (FieldOut::stats) */
 constexpr int STATS_WORDS = 24;
@@ -112,8 +135,9 @@ constexpr double POLISH_MOVE_LISTED = 1e-2;      /* theta_star: the same for an 
    unconverged; the polish, which always follows them, removes the mark. */
 CCF_HD double unconverged_mark(double err) { return isfinite(err) && err >= 0 ? -1 - err : err; }
 
-/* the fields of a polish launch: every point of every field, or (nbs > 0)
-   the columns [k0, k0 + nks) of branches [b0, b0 + nbs) */
+/* the fields of a polish launch: every point of every field's output
+   window, or (nbs > 0) the columns [k0, k0 + nks) of branches
+   [b0, b0 + nbs), which the window must hold */
 struct PolishArgs
 {
 	const FieldView* fields;

@@ -158,6 +158,7 @@ extern "C" ccf_status ccf_continue_branch_noalloc(ccf_handle* h, int branch, int
 	o.half = half;
 	o.step_first = 1;
 	o.step_last = num_steps;
+	ccf::full_window(o);
 	o.seg = 1;
 	o.max_iters_init = p.max_iters_init;
 	o.max_iters_step = p.max_iters_step;

@@ -105,9 +105,9 @@ bool check_params(const ccf_params& p, bool star_input, std::string& msg)
 		msg = "Error. init_cluster must be 0 (automatic), 1, 2, 4, 8 or 16.";
 		return false;
 	}
-	if (p.host_outputs != 0 && p.host_outputs != 1)
+	if (p.host_outputs < 0 || p.host_outputs > 2)
 	{
-		msg = "Error. host_outputs must be 0 or 1.";
+		msg = "Error. host_outputs must be 0, 1 or 2.";
 		return false;
 	}
 	if (p.autotune < 0 || p.autotune > 2)

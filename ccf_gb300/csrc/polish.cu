@@ -191,9 +191,10 @@ __device__ __noinline__ PolishOutcome polish_point(const FieldView& F, const Fie
 {
 	const int lane = threadIdx.x & 31;
 	const bool writer = WARP ? lane == 0 : true;
-	const size_t row = idx / (size_t)O.cols;
-	const int k = (int)(idx - row * (size_t)O.cols);
-	const int b = (int)(row % (size_t)O.nb);
+	/* branch and column of the window slot idx */
+	const size_t row = idx / (size_t)O.w_cols;
+	const int k = O.w_k0 + (int)(idx - row * (size_t)O.w_cols);
+	const int b = (O.w_b0 + (int)(row % (size_t)O.w_nb)) % O.nb;
 	double sp, cp;
 	sincos(column_phase(O, b, k), &sp, &cp);
 	const double2 z0 = O.ccs[idx];
@@ -360,8 +361,8 @@ __global__ void __launch_bounds__(256) polish_scan_kernel(const PolishArgs A)
 	const FieldView& F = sF;
 	const FieldOut& O = sO;
 	const bool box = A.nbs > 0;
-	const int b0 = box ? A.b0 : 0, nbs = box ? A.nbs : O.nb;
-	const int k0 = box ? A.k0 : 0, nks = box ? A.nks : O.cols;
+	const int b0 = box ? A.b0 : O.w_b0, nbs = box ? A.nbs : O.w_nb;
+	const int k0 = box ? A.k0 : O.w_k0, nks = box ? A.nks : O.w_cols;
 	const size_t per_root = (size_t)nbs * nks;
 	const size_t npts = (size_t)F.num_roots * per_root;
 	const size_t stride = (size_t)gridDim.x * blockDim.x;
@@ -372,13 +373,14 @@ __global__ void __launch_bounds__(256) polish_scan_kernel(const PolishArgs A)
 	for (size_t base = ((size_t)blockIdx.x * (blockDim.x >> 5) + warp) * 32; base < npts; base += stride)
 	{
 		const size_t i = base + lane;
-		const bool v = i < npts;
+		bool v = i < npts;
 		size_t idx = 0;
 		if (v)
 		{
 			const size_t a = i / per_root, r = i - a * per_root;
-			const size_t bb = b0 + r / nks, kk = k0 + r % nks;
-			idx = (a * O.nb + bb) * O.cols + kk;
+			const int bb = (int)((b0 + r / nks) % (size_t)O.nb), kk = (int)(k0 + r % nks);
+			idx = out_slot(O, (int)a, bb, kk);
+			v = idx != NO_OUT;
 		}
 		double e = v ? O.errs[idx] : 0;
 		const bool flag = v && !(e >= 0 && e <= POLISH_ERR);

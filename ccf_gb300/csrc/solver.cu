@@ -220,10 +220,13 @@ __device__ __noinline__ bool point_epilogue_warp(const FieldView& F, const Field
 	else pr = eval_point<false, false>(F, leaf, z, cphi, sphi, ns);
 	/* an unconverged point is marked for the FP64 polish (polish.cu) */
 	const double stored = unconv ? unconverged_mark(pr.err) : pr.err;
-	O.ccs[out] = z;
-	O.errs[out] = stored;
-	if (O.caustics) O.caustics[out] = pr.w;
-	if (mu) O.mu[out] = pr.mu_length;
+	if (out != NO_SLOT)
+	{
+		O.ccs[out] = z;
+		O.errs[out] = stored;
+		if (O.caustics) O.caustics[out] = pr.w;
+		if (mu) O.mu[out] = pr.mu_length;
+	}
 	if (out2 != NO_SLOT)
 	{
 		O.ccs[out2] = z;
@@ -654,8 +657,8 @@ __global__ void __launch_bounds__(NT, 2) solve_kernel(const SolveArgs A, const i
 			const int K = min(s_noff, OFF_CAP);
 			if (sO.mu) offfield_sums_cta<MIXED, true, true>(F, s_offz, K, s_offs, red_off);
 			else offfield_sums_cta<MIXED, true, false>(F, s_offz, K, s_offs, red_off);
-			const size_t out = ((size_t)(v ? a : 0) * nb + ob[0]) * sO.cols + ok[0];
-			const size_t out2 = nslot > 1 ? ((size_t)(v ? a : 0) * nb + ob[1]) * sO.cols + ok[1] : NO_SLOT;
+			const size_t out = out_slot(sO, v ? a : 0, ob[0], ok[0]);
+			const size_t out2 = nslot > 1 ? out_slot(sO, v ? a : 0, ob[1], ok[1]) : NO_SLOT;
 			const NearSums off = slot >= 0 ? s_offs[slot] : zero_sums();
 			const bool unconv = v && fin[a] != 1;
 			if (!point_epilogue_warp<MIXED>(F, sO, v, z, leaf, slot >= 0, off, out, out2, cphi, sphi, &s_maxerr, unconv))
@@ -1296,8 +1299,8 @@ __global__ void __launch_bounds__(TNT, 3) track_kernel(const TrackArgs T)
 						esp = sp;
 						int ob[2], ok[2];
 						const int nslot = row_slots(nb, O.half, O.seg, c, side, j, ob, ok);
-						out = ((size_t)a * nb + ob[0]) * O.cols + ok[0];
-						if (nslot > 1) out2 = ((size_t)a * nb + ob[1]) * O.cols + ok[1];
+						out = out_slot(O, a, ob[0], ok[0]);
+						if (nslot > 1) out2 = out_slot(O, a, ob[1], ok[1]);
 						if constexpr (MIXED)
 						{
 							if (!direct_out)
@@ -1329,9 +1332,12 @@ __global__ void __launch_bounds__(TNT, 3) track_kernel(const TrackArgs T)
 								const double err = fmax(fabs(af * (af + 2 * av)), fabs(af * (af - 2 * av)));
 								/* a stalled root is marked for the FP64 polish (polish.cu) */
 								const double stored = stuck ? unconverged_mark(err) : err;
-								O.ccs[out] = zf;
-								O.errs[out] = stored;
-								if (O.caustics) O.caustics[out] = wv;
+								if (out != NO_SLOT)
+								{
+									O.ccs[out] = zf;
+									O.errs[out] = stored;
+									if (O.caustics) O.caustics[out] = wv;
+								}
 								if (out2 != NO_SLOT)
 								{
 									O.ccs[out2] = zf;

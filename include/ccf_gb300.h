@@ -126,12 +126,15 @@ typedef struct ccf_params
 	                                of this shape (init_cluster, solved_centres), tuning on the
 	                                first run of a shape; 2: also expansion_order and
 	                                leaf_max_stars.  0 (default): the settings as given */
-	int host_outputs;            /* 1: the outputs (roots, caustics, 1/mu errors, length scales)
-	                                are written by the kernels straight into page-locked host
-	                                memory that the library holds, mapped into the GPU's address
-	                                space: they take no device memory and need no copy after the
-	                                run (on GB300 the GPU writes it over NVLink-C2C).  0 (default):
-	                                device memory */
+	int host_outputs;            /* where the outputs (roots, caustics, 1/mu errors, length
+	                                scales) are kept: 0 (default) device memory; 1 page-locked
+	                                host memory that the library holds, mapped into the GPU's
+	                                address space, written by the kernels directly (on GB300 over
+	                                NVLink-C2C): no device memory for them, no copy after the
+	                                run; 2 the same host memory, filled one group of branches at
+	                                a time from two device chunk buffers (about 2 GiB each) by
+	                                bulk copies that overlap the next group's computation (a
+	                                single field per run; batches write as with 1) */
 	int reserved[1];
 } ccf_params;
 

@@ -131,3 +131,25 @@ def test_host_outputs_are_the_same_bits_without_device_output_memory():
                                        ctypes.byref(mu)) == 0
     host_errs = np.ctypeslib.as_array(ctypes.cast(errs.value, ctypes.POINTER(ctypes.c_double)), shape=(pts,))
     assert np.array_equal(host_errs.reshape(ra["errs"].shape), ra["errs"])
+
+
+@pytest.mark.parametrize("continuation,centres", [("track", 4), ("aberth", 0)])
+def test_streamed_outputs_are_the_same_bits(monkeypatch, continuation, centres):
+    """host_outputs = 2: the continuation runs one group of solved centres at
+    a time into two device chunk buffers that are copied to host memory while
+    the next group computes.  With a small chunk target every centre is a
+    group of its own; with 4 solved centres of 32 branches each group's
+    window spans 9 branches, and the first one wraps around branch 0.  The
+    results are bit for bit those of device outputs."""
+    monkeypatch.setenv("CCF_GB300_CHUNK_BYTES", "1")
+    cfg = dict(CFG1, num_stars=800, num_phi=512, random_seed=99)
+    extra = dict(continuation=continuation, solved_centres=centres)
+    a = run(cfg, **extra)
+    b = run(cfg, host_outputs=2, **extra)
+    ia, ib = a.info(), b.info()
+    assert ib["centres_solved"] == ia["centres_solved"]
+    assert ia["rows_rerun"] == 0 and ib["rows_rerun"] == 0
+    ra, rb = a.results(stars=False), b.results(stars=False)
+    for k in ("ccs", "caustics", "errs"):
+        assert np.array_equal(ra[k], rb[k]), k
+    assert ib["max_error"] == ia["max_error"] and ib["unconverged"] == ia["unconverged"]
