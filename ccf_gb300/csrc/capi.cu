@@ -208,7 +208,8 @@ ccf_status ccf_host_alloc(size_t bytes, void** out)
 		cudaGetLastError();
 		return CCF_ERR_NO_DEVICE;
 	}
-	if (cudaHostAlloc(out, bytes > 0 ? bytes : 1, cudaHostAllocDefault) != cudaSuccess)
+	/* mapped and portable: the library's copy kernel can write it from any device */
+	if (cudaHostAlloc(out, bytes > 0 ? bytes : 1, cudaHostAllocMapped | cudaHostAllocPortable) != cudaSuccess)
 	{
 		cudaGetLastError();
 		*out = nullptr;

@@ -825,7 +825,8 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		   next to neighbouring stars, in the same or adjacent leaves, so their
 		   near-star loops and smooth-mass paths agree (the order of the roots
 		   within a column carries no meaning; a row stays one root's path) */
-		launch_seed_roots(s, N, R, K, f.star_pos.ptr, f.view.corner_abs, P.master_init.ptr + init_off[i],
+		launch_seed_roots(s, N, R, K, f.star_pos.ptr, f.star_mass.ptr, f.view.corner_abs, f.view.theta,
+			1 - f.view.kappa_tot + f.view.kappa_star, f.view.shear, nb, g, P.master_init.ptr + init_off[i],
 			mixed ? P.snap32_init.ptr + init_off[i] : nullptr, mixed ? nullptr : P.snap64_init.ptr + init_off[i]);
 	}
 	/* largest rows first */
@@ -1166,23 +1167,54 @@ ccf_status Engine::run(std::vector<Field*>& fields, int verbose)
 	return rc;
 }
 
+/* device array -> page-locked host memory mapped into the device's address
+   space, by the SMs: 16-byte loads and stores, every SM (on GB300 the stores
+   cross NVLink-C2C as full lines, faster than the copy engines' DMA) */
+__global__ void copy_to_host_kernel(const uint4* __restrict__ src, uint4* __restrict__ dst, size_t n16)
+{
+	const size_t stride = (size_t)gridDim.x * blockDim.x;
+	for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += stride) dst[i] = __ldcs(src + i);
+}
+
+/* copy bytes from device memory to host memory dst: by the copy kernel when
+   dst is page-locked, mapped and 16-byte aligned, else by cudaMemcpy */
+cudaError_t Engine::copy_out(void* dst, const void* src, size_t bytes)
+{
+	cudaPointerAttributes a;
+	const bool kernel = bytes >= (1u << 20) && ((uintptr_t)dst & 15) == 0 && ((uintptr_t)src & 15) == 0 && bytes % 16 == 0 &&
+		cudaPointerGetAttributes(&a, dst) == cudaSuccess && a.type == cudaMemoryTypeHost && a.devicePointer != nullptr;
+	cudaGetLastError();
+	if (!kernel) return cudaMemcpy(dst, src, bytes, cudaMemcpyDefault);
+	const int blocks = 4 * num_sms;
+	copy_to_host_kernel<<<blocks, 256, 0, stream>>>((const uint4*)src, (uint4*)a.devicePointer, bytes / 16);
+	cudaError_t e = cudaGetLastError();
+	if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+	return e;
+}
+
 ccf_status Engine::copy_results(Field& f, double* ccs, double* caustics, double* errs, double* mu, double* stars)
 {
 	if (!f.ran) { error = "Error. No results: run() has not completed."; return CCF_ERR_NOT_RUN; }
 	const size_t npts = (size_t)f.d.num_roots * f.params.num_branches * (f.params.num_phi / f.params.num_branches + 1);
-	/* the outputs sit in device memory or (host_outputs) page-locked host memory */
-	if (ccs) CCF_TRY(cudaMemcpy(ccs, f.out_ccs, npts * sizeof(double2), cudaMemcpyDefault), "copy ccs");
-	if (errs) CCF_TRY(cudaMemcpy(errs, f.out_errs, npts * sizeof(double), cudaMemcpyDefault), "copy errs");
-	if (caustics)
+	/* the outputs sit in device memory, or (host_outputs) page-locked host
+	   memory, which a plain copy reads */
+	auto copy = [&](void* dst, const void* src, size_t bytes) {
+		return f.params.host_outputs ? cudaMemcpy(dst, src, bytes, cudaMemcpyDefault) : copy_out(dst, src, bytes);
+	};
+	if (caustics && !f.params.write_caustics)
 	{
-		if (!f.params.write_caustics) { error = "Error. Caustics were not requested (write_caustics = 0)."; return CCF_ERR_INVALID_ARGUMENT; }
-		CCF_TRY(cudaMemcpy(caustics, f.out_caustics, npts * sizeof(double2), cudaMemcpyDefault), "copy caustics");
+		error = "Error. Caustics were not requested (write_caustics = 0).";
+		return CCF_ERR_INVALID_ARGUMENT;
 	}
-	if (mu)
+	if (mu && !f.params.write_mu_length_scales)
 	{
-		if (!f.params.write_mu_length_scales) { error = "Error. Length scales were not requested (write_mu_length_scales = 0)."; return CCF_ERR_INVALID_ARGUMENT; }
-		CCF_TRY(cudaMemcpy(mu, f.out_mu, npts * sizeof(double), cudaMemcpyDefault), "copy mu");
+		error = "Error. Length scales were not requested (write_mu_length_scales = 0).";
+		return CCF_ERR_INVALID_ARGUMENT;
 	}
+	if (ccs) CCF_TRY(copy(ccs, f.out_ccs, npts * sizeof(double2)), "copy ccs");
+	if (errs) CCF_TRY(copy(errs, f.out_errs, npts * sizeof(double)), "copy errs");
+	if (caustics) CCF_TRY(copy(caustics, f.out_caustics, npts * sizeof(double2)), "copy caustics");
+	if (mu) CCF_TRY(copy(mu, f.out_mu, npts * sizeof(double)), "copy mu");
 	if (stars)
 	{
 		const int N = f.d.num_stars;

@@ -225,6 +225,7 @@ public:
 	ccf_status run(std::vector<Field*>& fields, int verbose);
 	ccf_status save(Field& f, int verbose);
 	ccf_status copy_results(Field& f, double* ccs, double* caustics, double* errs, double* mu, double* stars);
+	cudaError_t copy_out(void* dst, const void* src, size_t bytes);
 
 	cudaStream_t stream = nullptr;
 	int device = 0;

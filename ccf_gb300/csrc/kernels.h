@@ -253,8 +253,9 @@ struct TrackArgs
 void launch_generate_stars(cudaStream_t s, int n, int seed, int rectangular, double2 corner, double corner_abs,
 	const MassTable& mt, double2* pos, double* mass);
 void launch_star_stats(cudaStream_t s, int n, const double* mass, double* out);
-void launch_seed_roots(cudaStream_t s, int nstars, int nroots, int nrows, const double2* pos, double corner_abs,
-	double2* master, float4* snap32, double2* snap64);
+void launch_seed_roots(cudaStream_t s, int nstars, int nroots, int nrows, const double2* pos, const double* mass,
+	double corner_abs, double theta, double a_lin, double gamma, int nb, int seg, double2* master, float4* snap32,
+	double2* snap64);
 void launch_star_hilo(cudaStream_t s, int n, const double2* pos, float4* out, const double* mass = nullptr,
 	float2* mass_out = nullptr);
 

@@ -84,21 +84,45 @@ __global__ void __launch_bounds__(1024) star_stats_kernel(int n, const double* _
 	}
 }
 
-/* Initial roots of a branch centre (include/ccf.cuh:711-726): z_i + 1 and
-   z_i - 1 for every star in generation order, then the extra roots of the
-   rectangular Taylor form evenly on the circle of radius |corner|.
-   Writes rows [row0, row0 + nrows) of master / snapshot. */
-__global__ void seed_roots_kernel(int nstars, int nroots, int nrows, const double2* __restrict__ pos, double corner_abs,
+/* Initial roots of the rows of solved branch centres (row r is the centre
+   of branch r seg).  Each star gets two seeds at the critical curve of the
+   star alone at the row's phase: with the star's own term the only one,
+   f = 0 reads theta^2 m / (z - z_i)^2 = a e^{-i phi} - gamma (a = 1 - kappa
+   - d alpha_smooth / dz, include/ccf_functions.cuh:69-86), so
+   z = z_i +/- theta sqrt(m) / sqrt(a e^{-i phi} - gamma).  The reference
+   seeds z_i +/- 1 (include/ccf.cuh:711-726); both lead the simultaneous
+   Aberth iteration to the same set of zeros, these in fewer sweeps.  The
+   extra roots of the rectangular Taylor form sit evenly on the circle of
+   radius |corner|, as in the reference.  Stars in tree order. */
+__global__ void seed_roots_kernel(int nstars, int nroots, int nrows, const double2* __restrict__ pos,
+	const double* __restrict__ mass, double corner_abs, double theta, double a_lin, double gamma, int nb, int seg,
 	double2* __restrict__ master, float4* __restrict__ snap32, double2* __restrict__ snap64)
 {
 	long long total = (long long)nrows * nroots;
 	int extra = nroots - 2 * nstars;
 	for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x)
 	{
+		const int row = (int)(q / nroots);
 		int a = (int)(q % nroots);
 		double2 z;
-		if (a < nstars) z = make_double2(pos[a].x + 1, pos[a].y);
-		else if (a < 2 * nstars) z = make_double2(pos[a - nstars].x - 1, pos[a - nstars].y);
+		if (a < 2 * nstars)
+		{
+			const int i = a < nstars ? a : a - nstars;
+			const double phi = PI / nb + (row * seg) * 2 * PI / nb;
+			double sp, cp;
+			sincos(phi, &sp, &cp);
+			/* D = a e^{-i phi} - gamma; w = theta sqrt(m) / sqrt(D) */
+			const double dx = a_lin * cp - gamma, dy = -a_lin * sp;
+			const double rd = hypot(dx, dy);
+			double2 w = make_double2(1, 0);
+			if (rd > 1e-6 && mass[i] > 0)
+			{
+				const double r = theta * sqrt(mass[i] / rd), t = -0.5 * atan2(dy, dx);
+				w = make_double2(r * cos(t), r * sin(t));
+			}
+			const double sg = a < nstars ? 1.0 : -1.0;
+			z = make_double2(pos[i].x + sg * w.x, pos[i].y + sg * w.y);
+		}
 		else
 		{
 			int i = a - 2 * nstars;
@@ -137,12 +161,14 @@ void launch_star_stats(cudaStream_t s, int n, const double* mass, double* out)
 	star_stats_kernel<<<1, 1024, 0, s>>>(n, mass, out);
 }
 
-void launch_seed_roots(cudaStream_t s, int nstars, int nroots, int nrows, const double2* pos, double corner_abs,
-	double2* master, float4* snap32, double2* snap64)
+void launch_seed_roots(cudaStream_t s, int nstars, int nroots, int nrows, const double2* pos, const double* mass,
+	double corner_abs, double theta, double a_lin, double gamma, int nb, int seg, double2* master, float4* snap32,
+	double2* snap64)
 {
 	long long total = (long long)nrows * nroots;
 	int blocks = (int)std::min<long long>((total + 255) / 256, 152 * 16);
-	seed_roots_kernel<<<blocks, 256, 0, s>>>(nstars, nroots, nrows, pos, corner_abs, master, snap32, snap64);
+	seed_roots_kernel<<<blocks, 256, 0, s>>>(nstars, nroots, nrows, pos, mass, corner_abs, theta, a_lin, gamma, nb, seg,
+		master, snap32, snap64);
 }
 
 void launch_star_hilo(cudaStream_t s, int n, const double2* pos, float4* out, const double* mass, float2* mass_out)

@@ -323,8 +323,9 @@ ccf_status Engine::solve_chunked(Field& f, int verbose)
 	const long long cap = std::min(1LL << 24, std::max(1LL << 16, (long long)(win_pts / 128)));
 	CCF_TRY_S(P.polish_list.ensure((size_t)cap + 1), "cudaMalloc(polish)");
 
-	launch_seed_roots(s, N, R, K, f.star_pos.ptr, f.view.corner_abs, P.master_init.ptr, mixed ? P.snap32_init.ptr : nullptr,
-		mixed ? nullptr : P.snap64_init.ptr);
+	launch_seed_roots(s, N, R, K, f.star_pos.ptr, f.star_mass.ptr, f.view.corner_abs, f.view.theta,
+		1 - f.view.kappa_tot + f.view.kappa_star, f.view.shear, nb, seg, P.master_init.ptr,
+		mixed ? P.snap32_init.ptr : nullptr, mixed ? nullptr : P.snap64_init.ptr);
 
 	auto polish = [&](const FieldOut* outs_dev, long long npts) -> cudaError_t {
 		cudaError_t e = cudaMemsetAsync(P.polish_list.ptr, 0, sizeof(unsigned long long), s);
