@@ -779,6 +779,7 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		o.step_first = 1;
 		o.step_last = o.half;
 		full_window(o);
+		o.check_inline = f.params.host_outputs == 1 ? 1 : 0;
 		o.max_iters_init = f.params.max_iters_init;
 		o.max_iters_step = f.params.max_iters_step;
 		o.seg = seg[i];
@@ -940,6 +941,7 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		CCF_TRY(cudaMemsetAsync(P.row_stats2.ptr, 0, TRACK_ROW_STATS * rc.size() * sizeof(unsigned long long), s), "memset");
 		CCF_TRY(launch_track_mark(s, T), "track_mark");
 		CCF_TRY(launch_track(s, T, mixed), "track_ccs");
+		CCF_TRY(launch_track_check(s, T, num_sms), "track_check");
 		CCF_TRY(launch_collect_rerun(s, T, P.rows_rerun.ptr, P.rerun_count.ptr), "collect_rerun");
 		/* rows that failed: tracked again from their centre with sub-steps of at
 		   most 1/TRACK_FINE_SUB of a phi step (the predictor's error falls as
@@ -955,6 +957,7 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		T2.counter = P.rerun_count.ptr + 4;
 		CCF_TRY(launch_clear_tables(s, T2), "clear_tables");
 		CCF_TRY(launch_track(s, T2, mixed), "track_ccs_fine");
+		CCF_TRY(launch_track_check(s, T2, num_sms), "track_check");
 		CCF_TRY(launch_collect_rerun(s, T2, P.rows_rerun2.ptr, P.rerun_count.ptr + 3), "collect_rerun");
 		A.rows = P.rows_rerun2.ptr;
 		A.num_rows_dev = P.rerun_count.ptr + 3;
@@ -992,11 +995,12 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 
 	ccf_status status = CCF_OK;
 	/* root seeds, initial solve, continuation (tracker: phase table, item
-	   marking, tracking, row collection, table clearing, re-tracking, row
-	   collection and the full-sum launch for the rows to re-run), FP64 polish */
+	   marking, tracking, column check, row collection, table clearing,
+	   re-tracking, column check, row collection and the full-sum launch for
+	   the rows to re-run), FP64 polish */
 	for (int fi = 0; fi < nf; fi++)
 	{
-		ccf_status rc = finish_stats(*fields[fi], seg[fi], track, verbose, track ? 12 : 5);
+		ccf_status rc = finish_stats(*fields[fi], seg[fi], track, verbose, track ? 14 : 5);
 		if (rc != CCF_OK) status = rc;
 	}
 	return status;

@@ -204,6 +204,9 @@ struct TrackConst
 	dfl shear, theta2, a, k1, kpi;
 	float2 ic, ic2;
 	float r2;
+	float aabs;            /* |a|, rounded up */
+	double w1x, w1y, wc1;  /* the lens map's linear terms with the Taylor or folded smooth-mass
+	                          forms: w = (w1x x + wc1, w1y y) + the star and series terms */
 };
 
 CCF_D TrackConst track_const(const FieldView& F)
@@ -217,6 +220,10 @@ CCF_D TrackConst track_const(const FieldView& F)
 	k.ic = make_float2((float)F.inv_corner.x, (float)F.inv_corner.y);
 	k.ic2 = make_float2((float)F.inv_corner2.x, (float)F.inv_corner2.y);
 	k.r2 = (float)(SMOOTH_DF_RANGE * F.corner_abs * F.corner_abs);
+	k.aabs = __fadd_ru(fabsf(k.a.hi), fabsf(k.a.lo));
+	k.w1x = 1 - F.kappa_tot + F.shear + 2 * F.kappa_star;
+	k.w1y = 1 - F.kappa_tot - F.shear;
+	k.wc1 = 2 * F.kappa_star * F.corner.x;
 	return k;
 }
 
@@ -244,8 +251,8 @@ struct TrackEval
 {
 	float2 step;      /* f / (f' + f pole) */
 	float as2;        /* |step|^2 */
-	double2 fz;       /* f in FP64 */
-	double af;        /* bound on |f| at the stepped root z - step: |f - f' step|,
+	float2 fz;        /* f, rounded to FP32 (the first-order output correction) */
+	float af;         /* bound on |f| at the stepped root z - step: |f - f' step|,
 	                     the FP32 error of f' step, the double-float rounding of
 	                     the terms of f and the FP64 spacing of the root times |f'| */
 	dfc wpart;
@@ -365,8 +372,8 @@ CCF_D TrackEval eval_track_df(const FieldView& F, const TrackConst& K, int leaf,
 	fi = df_add(fi, df_neg(dl.im));
 	fi = df_add(fi, ds.im);
 	fi = df_add(fi, df_mul(a, sph));
-	e.fz = dfc_to({fr, fi});
 	const float2 f32 = make_float2(fr.hi + fr.lo, fi.hi + fi.lo);
+	e.fz = f32;
 	const float t2 = K.theta2.hi;
 	const float2 df = make_float2(-2 * t2 * s3.x - d2l.x - d2s.x, -2 * t2 * s3.y - d2l.y + d2s.y);
 	pole = make_float2(2.f * pole.x, 2.f * pole.y);
@@ -383,13 +390,14 @@ CCF_D TrackEval eval_track_df(const FieldView& F, const TrackConst& K, int leaf,
 	/* |f| at z - st: f - f' st (f holomorphic), the FP32 error of f' st, the
 	   double-float rounding of the terms of f (2^-47 of their sizes) and half
 	   the FP64 spacing of the root times |f'|.  The difference is formed in
-	   FP64 and its modulus taken in FP32, rounded up by 2^-20 (the FP32
-	   roundings of the sum are a few 2^-24): a bound, not an estimate */
+	   FP32 from f's double-float parts: (hi - f' st) + lo errs by 2^-23 of the
+	   result plus 2^-48 |f| (the 3.6e-15 |f| term); the sum is rounded up by
+	   2^-20 (its FP32 roundings are a few 2^-24): a bound, not an estimate */
 	const float2 fsv = fmulc(df, st);
 	const float terms = t2 * tabs + hypotf(dl.re.hi, dl.im.hi) + hypotf(ds.re.hi, ds.im.hi) + fabsf(a.hi) + fabsf(K.shear.hi);
-	const float res = hypotf((float)(e.fz.x - (double)fsv.x), (float)(e.fz.y - (double)fsv.y));
-	e.af = (double)((res + 1e-6f * hypotf(fsv.x, fsv.y) + 7.2e-15f * terms + 1.2e-16f * hypotf(zx, zy) * hypotf(df.x, df.y)) *
-		(1.f + 0x1p-20f));
+	const float res = hypotf(__fadd_rn(__fsub_rn(fr.hi, fsv.x), fr.lo), __fadd_rn(__fsub_rn(fi.hi, fsv.y), fi.lo));
+	e.af = (res + 1e-6f * hypotf(fsv.x, fsv.y) + 3.6e-15f * hypotf(f32.x, f32.y) + 7.2e-15f * terms +
+		1.2e-16f * hypotf(zx, zy) * hypotf(df.x, df.y)) * (1.f + 0x1p-20f);
 	/* w - the linear terms: (-theta^2 s1.x - al.x - sa.x, theta^2 s1.y + al.y - sa.y) (eval_point_df) */
 	dfl wr = df_neg(df_mul(K.theta2, s1.re));
 	wr = df_add(wr, df_neg(al.re));

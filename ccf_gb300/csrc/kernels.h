@@ -84,6 +84,10 @@ struct FieldOut
 	   (mod nb) and columns w_k0 .. w_k0 + w_cols - 1 of each, in the file
 	   layout's order; the whole field is (0, nb, 0, cols) */
 	int w_b0, w_nb, w_k0, w_cols;
+	/* tracker: 1 when the outputs lie in host memory, where the column check
+	   runs inside the tracking launch; else a launch of its own reads the
+	   stored roots back (track_check_kernel) */
+	int check_inline;
 	/* statistics */
 	unsigned long long* stats;   /* STATS_WORDS words: [0] max_err bits, [1] nan flag, [2] updates,
 	                                [3] terms, [4] unconverged, [5] max sweeps init, [6] max sweeps
@@ -291,6 +295,7 @@ cudaError_t launch_solve(cudaStream_t s, const SolveArgs& a, bool mixed, bool in
 cudaError_t launch_track_mark(cudaStream_t s, const TrackArgs& a);
 cudaError_t launch_phase_table(cudaStream_t s, int nb, int nphi, PhaseEntry* out);
 cudaError_t launch_track(cudaStream_t s, const TrackArgs& a, bool mixed);
+cudaError_t launch_track_check(cudaStream_t s, const TrackArgs& a, int num_sms);
 cudaError_t launch_collect_rerun(cudaStream_t s, const TrackArgs& a, RowDesc* rerun, int* count);
 cudaError_t launch_clear_tables(cudaStream_t s, const TrackArgs& a);
 cudaError_t launch_eval_points(cudaStream_t s, const FieldView* F_dev, int npts, const double2* z, const double* phi,

@@ -922,14 +922,14 @@ CCF_D void offfield_sums_warp_df(const FieldView& F, bool need, double2 z, NearS
    Kept out of line, as the rare path of the iteration.  All 32 lanes must
    call it. */
 __device__ __noinline__ TrackEval track_offfield(const FieldView& F, bool off, double2 z, double cphi, double sphi,
-	bool disc_exact)
+	bool disc_exact, float wtol2)
 {
 	NearSums ns = zero_sums();
 	offfield_sums_warp_df<true, true>(F, off, z, ns);
 	TrackEval r;
 	r.step = make_float2(0.f, 0.f);
 	r.as2 = 0;
-	r.fz = make_double2(0, 0);
+	r.fz = make_float2(0.f, 0.f);
 	r.af = 0;
 	r.wpart = {{0.f, 0.f}, {0.f, 0.f}};
 	r.wmode = 2;
@@ -946,13 +946,15 @@ __device__ __noinline__ TrackEval track_offfield(const FieldView& F, bool off, d
 	r.step = make_float2((float)st.x, (float)st.y);
 	const double as2 = st.x * st.x + st.y * st.y;
 	r.as2 = as2 < 3e38 ? (float)as2 : INFINITY;   /* a step beyond the FP32 range fails */
-	r.fz = f;
+	r.fz = make_float2((float)f.x, (float)f.y);
 	const double2 fs = cmul(df, make_double2(r.step.x, r.step.y));
 	const double2 ds = smooth_dzbar(F, z);
-	r.af = hypot(f.x - fs.x, f.y - fs.y) +
+	r.af = __double2float_ru(hypot(f.x - fs.x, f.y - fs.y) +
 		7.2e-15 * (F.theta2 * hypot(ns.s2.x, ns.s2.y) + hypot(ds.x, ds.y) + 1 + F.shear) +
-		1.2e-16 * hypot(z.x, z.y) * hypot(df.x, df.y);
-	r.wpart = dfc_from(eval_point_df(F, -1, z, cphi, sphi, ns).w);
+		1.2e-16 * hypot(z.x, z.y) * hypot(df.x, df.y));
+	/* the lens map only where the point can be final: a step below the
+	   tolerance, or a stalled root kept as it is */
+	if (r.as2 < wtol2) r.wpart = dfc_from(eval_point_df(F, -1, z, cphi, sphi, ns).w);
 	return r;
 }
 
@@ -1152,6 +1154,7 @@ __global__ void __launch_bounds__(TNT, 3) track_kernel(const TrackArgs T)
 		const double inv_cell = CELL_PER_THETA / F.theta;
 		const unsigned long long slots = 2ull * (unsigned long long)R;
 		const bool direct_out = !MIXED || O.mu != nullptr;
+		unsigned long long lane_maxerr = 0;   /* bits of the lane's largest 1/mu bound (non-negative) */
 
 		double2 z1 = valid ? T.master[RD.base + a] : make_double2(0, 0);
 		int t1 = (j0 - 1) * TSUB;
@@ -1194,7 +1197,7 @@ __global__ void __launch_bounds__(TNT, 3) track_kernel(const TrackArgs T)
 			TrackEval e;
 			e.step = make_float2(0.f, 0.f);
 			e.as2 = 0;
-			e.fz = make_double2(0, 0);
+			e.fz = make_float2(0.f, 0.f);
 			e.af = 0;
 			e.wpart = {{0.f, 0.f}, {0.f, 0.f}};
 			e.wmode = 2;
@@ -1203,7 +1206,7 @@ __global__ void __launch_bounds__(TNT, 3) track_kernel(const TrackArgs T)
 				if (act && leaf >= 0) e = eval_track_df(F, K, leaf, z, rel, cpd, spd, disc_exact);
 				if (__any_sync(full, off))
 				{
-					const TrackEval o = track_offfield(F, off, z, cp, sp, disc_exact);
+					const TrackEval o = track_offfield(F, off, z, cp, sp, disc_exact, (float)stuck2);
 					if (off) e = o;
 				}
 				step = make_double2((double)e.step.x, (double)e.step.y);
@@ -1305,31 +1308,48 @@ __global__ void __launch_bounds__(TNT, 3) track_kernel(const TrackArgs T)
 						{
 							if (!direct_out)
 							{
-								/* the lens map at the evaluated point, then corrected to
-								   zf = ze - s: w(zf) = w(ze) - a s - (conj(f) + a e^{i phi}) conj(s) */
-								const double2 ze = make_double2(zf.x + step.x, zf.y + step.y);
-								double2 wv;
-								if (e.wmode == 2) wv = dfc_to(e.wpart);
+								/* the lens map at the evaluated point ze, corrected to zf = ze - s:
+								   w(zf) = w(ze) - a s - (conj(f) + a e^{i phi}) conj(s).  With
+								   |s| below 1e-9 theta_star the correction and the linear terms'
+								   share a s are FP32; the rest sums in FP64 at zf */
+								const float sx = e.step.x, sy = e.step.y;
+								double av = 0;
+								float avf = K.a.hi;
+								if (!F.approx)
+								{
+									av = 1 - F.kappa_tot - smooth_dz(F, make_double2(zf.x + step.x, zf.y + step.y));
+									avf = (float)av;
+								}
+								double wx, wy;
+								float lx = 0.f, ly = 0.f;   /* the linear terms' coefficients of s */
+								if (e.wmode == 2)
+								{
+									wx = df_to_double(e.wpart.re);
+									wy = df_to_double(e.wpart.im);
+								}
+								else if (e.wmode == 1)
+								{
+									wx = fma(K.w1x, zf.x, (double)e.wpart.re.hi) + ((double)e.wpart.re.lo + K.wc1);
+									wy = fma(K.w1y, zf.y, (double)e.wpart.im.hi) + (double)e.wpart.im.lo;
+									lx = (float)K.w1x;
+									ly = (float)K.w1y;
+								}
 								else
 								{
+									const double2 ze = make_double2(zf.x + step.x, zf.y + step.y);
 									const double2 wp = dfc_to(e.wpart);
-									wv.x = (1 - F.kappa_tot + F.shear) * ze.x + wp.x;
-									wv.y = (1 - F.kappa_tot - F.shear) * ze.y + wp.y;
-									if (e.wmode == 1) wv.x += 2 * F.kappa_star * (F.corner.x + ze.x);
-									else
-									{
-										const double2 sa = smooth_alpha(F, ze);
-										wv.x -= sa.x;
-										wv.y -= sa.y;
-									}
+									const double2 sa = smooth_alpha(F, ze);
+									wx = (1 - F.kappa_tot + F.shear) * ze.x + wp.x - sa.x;
+									wy = (1 - F.kappa_tot - F.shear) * ze.y + wp.y - sa.y;
 								}
-								const double av = 1 - F.kappa_tot - smooth_dz(F, ze);
-								const double2 fz = e.fz;
-								const double gx = fz.x + av * cp, gy = -fz.y + av * sp;
-								wv.x -= av * step.x + gx * step.x + gy * step.y;
-								wv.y -= av * step.y - gx * step.y + gy * step.x;
-								const double af = e.af;
-								const double err = fmax(fabs(af * (af + 2 * av)), fabs(af * (af - 2 * av)));
+								const float gx = e.fz.x + avf * cpd.hi, gy = -e.fz.y + avf * spd.hi;
+								const float cx = lx * sx - (avf * sx + gx * sx + gy * sy);
+								const float cy = ly * sy - (avf * sy - gx * sy + gy * sx);
+								const double2 wv = make_double2(wx + (double)cx, wy + (double)cy);
+								/* max(|af (af + 2 a)|, |af (af - 2 a)|) = af (af + 2 |a|), rounded up */
+								const float aabs = F.approx ? K.aabs : __double2float_ru(fabs(av));
+								const float af = e.af;
+								const double err = (double)__fmul_ru(af, __fadd_ru(af, __fmul_ru(2.f, aabs)));
 								/* a stalled root is marked for the FP64 polish (polish.cu) */
 								const double stored = stuck ? unconverged_mark(err) : err;
 								if (out != NO_SLOT)
@@ -1344,12 +1364,16 @@ __global__ void __launch_bounds__(TNT, 3) track_kernel(const TrackArgs T)
 									O.errs[out2] = stored;
 									if (O.caustics) O.caustics[out2] = wv;
 								}
-								if (isfinite(err)) atomicMax((unsigned long long*)&s_maxerr[w], (unsigned long long)__double_as_longlong(err));
+								if (isfinite(err)) lane_maxerr = max(lane_maxerr, (unsigned long long)__double_as_longlong(err));
 								else flags |= (unsigned)TRACK_NONFINITE;
 							}
 						}
-						flags |= (unsigned)table_insert(T.table + RD.cont_base + (size_t)(j - j0) * slots, slots,
-							cell_key(zf, inv_cell));
+						/* the column check: by track_check_kernel after the launch, from
+						   the stored root, unless the outputs lie in host memory or the
+						   window does not hold this column */
+						if (O.check_inline || out == NO_OUT)
+							flags |= (unsigned)table_insert(T.table + RD.cont_base + (size_t)(j - j0) * slots, slots,
+								cell_key(zf, inv_cell));
 						maxev = max(maxev, evs);
 						evs = 0;
 						j++;
@@ -1409,6 +1433,7 @@ __global__ void __launch_bounds__(TNT, 3) track_kernel(const TrackArgs T)
 			}
 		}
 		if (valid && lost) flags |= (unsigned)TRACK_LOST;
+		for (int o = 16; o > 0; o >>= 1) lane_maxerr = max(lane_maxerr, __shfl_xor_sync(full, lane_maxerr, o));
 		unconv = __reduce_add_sync(full, unconv);
 		flags = __reduce_or_sync(full, flags);
 		maxev = (int)__reduce_max_sync(full, (unsigned)maxev);
@@ -1418,7 +1443,7 @@ __global__ void __launch_bounds__(TNT, 3) track_kernel(const TrackArgs T)
 		if (lane == 0)
 		{
 			unsigned long long* rs = T.row_stats + TRACK_ROW_STATS * (size_t)row;
-			atomicMax(&rs[0], (unsigned long long)__double_as_longlong(s_maxerr[w]));
+			atomicMax(&rs[0], max(lane_maxerr, (unsigned long long)__double_as_longlong(s_maxerr[w])));
 			if (flags) atomicOr(&rs[1], (unsigned long long)flags);
 			atomicMax(&rs[2], (unsigned long long)maxev);
 			if (unconv) atomicAdd(&rs[3], (unsigned long long)unconv);
@@ -1503,6 +1528,52 @@ __global__ void clear_tables_kernel(const TrackArgs T)
 			i += (unsigned long long)gridDim.x * blockDim.x)
 			tab[i] = 0ull;
 	}
+}
+
+/* The column check of a tracking launch, after it: every (row, phi step)
+   column's stored roots go into that column's table of 2^-20 theta_star
+   cells, and a cell taken twice (two roots of the row converged to one zero)
+   flags the row, as the tracker's own insert would.  One thread per stored
+   point, the steps of a root in consecutive threads (consecutive columns of
+   the output layout); every block walks the rows in order, so the tables in
+   use at a time stay in L2.  Points whose column the output window does not
+   hold, and fields with outputs in host memory, were checked by the tracker
+   itself.  A lost root leaves stale values in its later columns, which can
+   only flag its own row, already flagged as lost. */
+__global__ void track_check_kernel(const TrackArgs T)
+{
+	const int nrows = T.num_rows_dev ? *T.num_rows_dev : T.num_rows;
+	for (int q = 0; q < nrows; q++)
+	{
+		const RowDesc RD = T.rows[q];
+		const FieldOut O = T.outs[RD.field];
+		if (O.check_inline) continue;
+		const int R = T.fields[RD.field].num_roots;
+		const double inv_cell = CELL_PER_THETA / T.fields[RD.field].theta;
+		const int j0 = O.step_first, nsteps = RD.steps - j0 + 1;
+		if (nsteps <= 0) continue;
+		const unsigned long long slots = 2ull * (unsigned long long)R;
+		const long long n = (long long)R * nsteps;
+		unsigned flags = 0;
+		for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+		{
+			const int a = (int)(i / nsteps), j = j0 + (int)(i - (long long)a * nsteps);
+			int ob[2], ok[2];
+			row_slots(O.nb, O.half, O.seg, RD.branch, RD.side, j, ob, ok);
+			const size_t out = out_slot(O, a, ob[0], ok[0]);
+			if (out == NO_OUT) continue;
+			flags |= (unsigned)table_insert(T.table + RD.cont_base + (size_t)(j - j0) * slots, slots,
+				cell_key(O.ccs[out], inv_cell));
+		}
+		if (flags) atomicOr(&T.row_stats[TRACK_ROW_STATS * (size_t)q + 1], (unsigned long long)flags);
+	}
+}
+
+cudaError_t launch_track_check(cudaStream_t s, const TrackArgs& a, int num_sms)
+{
+	if (a.num_rows == 0) return cudaSuccess;
+	track_check_kernel<<<num_sms * 8, 256, 0, s>>>(a);
+	return cudaGetLastError();
 }
 
 cudaError_t launch_clear_tables(cudaStream_t s, const TrackArgs& a)
