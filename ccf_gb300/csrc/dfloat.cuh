@@ -100,15 +100,32 @@ CCF_D dfl df_add_fast(dfl a, dfl b)
 	return fast_two_sum(s.hi, s.lo);
 }
 
-/* 1/a: FP32 estimate q1, residual 1 - a q1 in double-float, one correction */
+/* 1/a: FP32 estimate q1, residual r = 1 - a q1, one correction q1 r.  a q1
+   is formed in double-float (p); p.hi lies within 2^-22 of 1, so 1 - p.hi is
+   exact and r needs FP32 accuracy only (q1 r is 2^-23 of the result) */
 CCF_D dfl df_rcp(dfl a)
 {
 	float q1 = rcp32(a.hi);
 	dfl p = df_mul_f(a, q1);
-	dfl r = df_add({1.0f, 0.0f}, df_neg(p));
-	float q2 = __fmul_rn(r.hi, q1);
+	float r = __fsub_rn(__fsub_rn(1.0f, p.hi), p.lo);
+	float q2 = __fmul_rn(r, q1);
 	return fast_two_sum(q1, q2);
 }
+
+/* running double-float sum: the leading parts add exactly (two_sum), the low
+   parts and those roundings collect in one FP32 word; dfacc_get
+   renormalises.  Error ~2^-48 of the sum of |terms| */
+struct dfacc
+{
+	float hi, lo;
+};
+CCF_D void dfacc_add(dfacc& a, dfl x)
+{
+	const dfl s = two_sum(a.hi, x.hi);
+	a.hi = s.hi;
+	a.lo = __fadd_rn(a.lo, __fadd_rn(s.lo, x.lo));
+}
+CCF_D dfl dfacc_get(dfacc a) { return fast_two_sum(a.hi, a.lo); }
 
 /* complex */
 CCF_D dfc dfc_from(double2 z) { return {df_from_double(z.x), df_from_double(z.y)}; }
@@ -119,6 +136,30 @@ CCF_D dfc dfc_mul(dfc a, dfc b)
 	return {df_add(df_mul(a.re, b.re), df_neg(df_mul(a.im, b.im))), df_add_fast(df_mul(a.re, b.im), df_mul(a.im, b.re))};
 }
 CCF_D dfc dfc_load(float4 v) { return {{v.x, v.z}, {v.y, v.w}}; }
+
+/* x y + u z + c, real double-float, one renormalisation: the products of the
+   leading parts and c's leading part sum exactly (two_prod, two_sum), every
+   lower-order term collects in one FP32 sum.  Error ~2^-47 of
+   |x y| + |u z| + |c| */
+CCF_D dfl df_dot2_add(dfl x, dfl y, dfl u, dfl z, dfl c)
+{
+	const float p = __fmul_rn(x.hi, y.hi);
+	const float pe = __fmaf_rn(x.hi, y.hi, -p);
+	const float q = __fmul_rn(u.hi, z.hi);
+	const float qe = __fmaf_rn(u.hi, z.hi, -q);
+	const dfl s = two_sum(p, q);
+	const dfl t = two_sum(s.hi, c.hi);
+	const float e1 = __fmaf_rn(x.lo, y.hi, __fmaf_rn(x.hi, y.lo, pe));
+	const float e2 = __fmaf_rn(u.lo, z.hi, __fmaf_rn(u.hi, z.lo, qe));
+	const float lo = __fadd_rn(__fadd_rn(e1, e2), __fadd_rn(__fadd_rn(s.lo, t.lo), c.lo));
+	return fast_two_sum(t.hi, lo);
+}
+
+/* a b + c, complex double-float (one Horner step) */
+CCF_D dfc dfc_fma(dfc a, dfc b, dfc c)
+{
+	return {df_dot2_add(a.re, b.re, df_neg(a.im), b.im, c.re), df_dot2_add(a.re, b.im, a.im, b.re, c.im)};
+}
 CCF_D float4 dfc_pack(dfc a) { return make_float4(a.re.hi, a.im.hi, a.re.lo, a.im.lo); }
 
 } /* namespace ccf */

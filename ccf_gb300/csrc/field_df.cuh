@@ -111,7 +111,7 @@ CCF_D void star_term_df(SumsDF& a, dfc& s3, float2& s3f, const dfc& z, float4 p,
 CCF_D dfc horner_df(const float4* L, int P, int first, dfc dz)
 {
 	dfc acc = dfc_load(L[P]);
-	for (int i = P - 1; i >= first; i--) acc = dfc_add(dfc_mul(acc, dz), dfc_load(L[i]));
+	for (int i = P - 1; i >= first; i--) acc = dfc_fma(acc, dz, dfc_load(L[i]));
 	return acc;
 }
 
@@ -274,7 +274,7 @@ CCF_D TrackEval eval_track_df(const FieldView& F, const TrackConst& K, int leaf,
 	bool disc_exact)
 {
 	const dfc zr = dfc_from(rel);
-	dfc s1 = {{0.f, 0.f}, {0.f, 0.f}}, s2 = s1;
+	dfacc s1r = {0.f, 0.f}, s1i = s1r, s2r = s1r, s2i = s1r;
 	float2 s3 = make_float2(0.f, 0.f), pole = make_float2(0.f, 0.f);
 	float tabs = 0.f;   /* sum of |m / d^2| */
 	const int n = F.leaf_near_count[leaf];
@@ -290,13 +290,14 @@ CCF_D TrackEval eval_track_df(const FieldView& F, const TrackConst& K, int leaf,
 		const dfl r = df_rcp(df_add_fast(df_sqr(dx), df_sqr(dy)));
 		const dfl ix = df_mul(dx, r);
 		const dfl iy = df_neg(df_mul(dy, r));                     /* 1/d */
-		const dfl i2x = df_add(df_sqr(ix), df_neg(df_sqr(iy)));
+		/* ix^2 - iy^2 to 2^-47 of 1/|d|^2, the size of the term */
+		const dfl i2x = df_add_fast(df_sqr(ix), df_neg(df_sqr(iy)));
 		dfl i2y = df_mul(ix, iy);
 		i2y = {2.f * i2y.hi, 2.f * i2y.lo};                        /* 1/d^2 */
-		s2.re = df_add_fast(s2.re, df_mul(m, i2x));
-		s2.im = df_add_fast(s2.im, df_mul(m, i2y));
-		s1.re = df_add_fast(s1.re, df_mul(m, ix));
-		s1.im = df_add_fast(s1.im, df_mul(m, iy));
+		dfacc_add(s2r, df_mul(m, i2x));
+		dfacc_add(s2i, df_mul(m, i2y));
+		dfacc_add(s1r, df_mul(m, ix));
+		dfacc_add(s1i, df_mul(m, iy));
 		pole.x += ix.hi;
 		pole.y += iy.hi;
 		const float i3x = i2x.hi * ix.hi - i2y.hi * iy.hi;
@@ -305,6 +306,7 @@ CCF_D TrackEval eval_track_df(const FieldView& F, const TrackConst& K, int leaf,
 		s3.y = fmaf(m.hi, i3y, s3.y);
 		tabs = fmaf(m.hi, fmaf(ix.hi, ix.hi, iy.hi * iy.hi), tabs);
 	}
+	const dfc s1 = {dfacc_get(s1r), dfacc_get(s1i)}, s2 = {dfacc_get(s2r), dfacc_get(s2i)};
 	const int P = F.order;
 	const float2 ihf = F.leaf_ih_df[leaf];
 	const dfl ih = {ihf.x, ihf.y};

@@ -934,7 +934,11 @@ __device__ __noinline__ TrackEval track_offfield(const FieldView& F, bool off, d
 	r.wpart = {{0.f, 0.f}, {0.f, 0.f}};
 	r.wmode = 2;
 	if (!off) return r;
-	const double2 f = eval_f_df(F, -1, z, cphi, sphi, ns);
+	/* f as eval_f_df and w as eval_point_df off the root box, with the
+	   smooth-mass d alpha / d zbar series evaluated once */
+	const double2 ds = smooth_dzbar_any(F, z);
+	const double a = 1 - F.kappa_tot - smooth_dz(F, z);
+	const double2 f = make_double2(F.shear + F.theta2 * ns.s2.x - ds.x - a * cphi, F.theta2 * ns.s2.y + ds.y + a * sphi);
 	const double2 df = eval_df_mixed(F, -1, z, ns.s3);
 	double2 S = make_double2(0, 0);
 	if (disc_exact)
@@ -948,13 +952,18 @@ __device__ __noinline__ TrackEval track_offfield(const FieldView& F, bool off, d
 	r.as2 = as2 < 3e38 ? (float)as2 : INFINITY;   /* a step beyond the FP32 range fails */
 	r.fz = make_float2((float)f.x, (float)f.y);
 	const double2 fs = cmul(df, make_double2(r.step.x, r.step.y));
-	const double2 ds = smooth_dzbar(F, z);
 	r.af = __double2float_ru(hypot(f.x - fs.x, f.y - fs.y) +
 		7.2e-15 * (F.theta2 * hypot(ns.s2.x, ns.s2.y) + hypot(ds.x, ds.y) + 1 + F.shear) +
 		1.2e-16 * hypot(z.x, z.y) * hypot(df.x, df.y));
 	/* the lens map only where the point can be final: a step below the
 	   tolerance, or a stalled root kept as it is */
-	if (r.as2 < wtol2) r.wpart = dfc_from(eval_point_df(F, -1, z, cphi, sphi, ns).w);
+	if (r.as2 < wtol2)
+	{
+		const double2 as = smooth_alpha_any(F, z);
+		const double2 w = make_double2((1 - F.kappa_tot) * z.x + F.shear * z.x - F.theta2 * ns.s1.x - as.x,
+			(1 - F.kappa_tot) * z.y - F.shear * z.y + F.theta2 * ns.s1.y - as.y);
+		r.wpart = dfc_from(w);
+	}
 	return r;
 }
 
