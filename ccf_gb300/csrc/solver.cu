@@ -915,6 +915,69 @@ CCF_D void offfield_sums_warp_df(const FieldView& F, bool need, double2 z, NearS
 	}
 }
 
+/* The FP64 smooth-mass series of the rectangular Taylor form at a point
+   outside the corner circle -- d alpha / d zbar and d2 alpha / d zbar2 in
+   u = (zbar / c)^2, alpha in zbar (smooth_dzbar, smooth_d2zbar,
+   smooth_alpha) -- evaluated by the 32 lanes together for one point: lane l
+   forms the terms l, l + 32, ... of each series from its powers u^l and
+   zbar^l (binary powering), and the partial sums meet by shuffles.  One
+   point's three series cost ~140 FP64 warp instructions in chains of ~20,
+   where one lane's Horner passes take ~460 in chains of ~115.  All 32 lanes
+   call it with the same z. */
+struct SmoothSeries
+{
+	double2 ds, d2s, alpha;
+};
+
+__device__ __noinline__ SmoothSeries smooth_series_warp(const FieldView& F, double2 z)
+{
+	const unsigned full = 0xffffffffu;
+	const int lane = threadIdx.x & 31;
+	const double2 zb = cconj(z);
+	const double2 r = cmul(zb, F.inv_corner);
+	const double2 u = cmul(r, r);
+	double2 ul = make_double2(1, 0), zl = make_double2(1, 0), up = u, zp = zb;
+	for (int b = 0; b < 5; b++)
+	{
+		if ((lane >> b) & 1)
+		{
+			ul = cmul(ul, up);
+			zl = cmul(zl, zp);
+		}
+		up = cmul(up, up);
+		zp = cmul(zp, zp);
+	}
+	double2 p1 = make_double2(0, 0), p2 = p1, pa = p1;
+	for (int m = lane; m < F.smooth_m; m += 32)
+	{
+		p1 = cadd(p1, cmul(F.smooth_d1[m], ul));
+		p2 = cadd(p2, cmul(F.smooth_d2[m], ul));
+		ul = cmul(ul, up);
+	}
+	const int n = F.taylor_smooth + 1;
+	for (int i = lane; i <= n; i += 32)
+	{
+		pa = cadd(pa, cmul(F.smooth_a[i], zl));
+		zl = cmul(zl, zp);
+	}
+	for (int o = 16; o > 0; o >>= 1)
+	{
+		p1.x += __shfl_xor_sync(full, p1.x, o);
+		p1.y += __shfl_xor_sync(full, p1.y, o);
+		p2.x += __shfl_xor_sync(full, p2.x, o);
+		p2.y += __shfl_xor_sync(full, p2.y, o);
+		pa.x += __shfl_xor_sync(full, pa.x, o);
+		pa.y += __shfl_xor_sync(full, pa.y, o);
+	}
+	SmoothSeries out;
+	out.ds = cmul(p1, u);
+	out.ds.x += F.smooth_k1;
+	out.d2s = cmul(p2, cmul(zb, F.inv_corner2));
+	out.alpha = cmul(pa, make_double2(0, -F.kappa_star / PI));
+	out.alpha.x -= F.kappa_star * 2 * (F.corner.x + z.x);
+	return out;
+}
+
 /* The iteration quantities of the tracker (TrackEval) for the warp's lanes
    with off set, which lie outside the root box: direct double-float sums over
    every star, then f, f', the step and the whole lens map (wmode 2) in FP64
@@ -924,8 +987,22 @@ CCF_D void offfield_sums_warp_df(const FieldView& F, bool need, double2 z, NearS
 __device__ __noinline__ TrackEval track_offfield(const FieldView& F, bool off, double2 z, double cphi, double sphi,
 	bool disc_exact, float wtol2)
 {
+	const unsigned full = 0xffffffffu;
+	const int lane = threadIdx.x & 31;
 	NearSums ns = zero_sums();
 	offfield_sums_warp_df<true, true>(F, off, z, ns);
+	/* the Taylor form's series outside the corner circle, warp-wide per point */
+	const bool series = F.rectangular && F.approx && F.smooth_m > 0 && !smooth_df_ok(F, z);
+	SmoothSeries sm;
+	sm.ds = sm.d2s = sm.alpha = make_double2(0, 0);
+	unsigned pend = __ballot_sync(full, off && series);
+	while (pend)
+	{
+		const int src = __ffs(pend) - 1;
+		pend &= pend - 1;
+		const SmoothSeries t = smooth_series_warp(F, make_double2(__shfl_sync(full, z.x, src), __shfl_sync(full, z.y, src)));
+		if (lane == src) sm = t;
+	}
 	TrackEval r;
 	r.step = make_float2(0.f, 0.f);
 	r.as2 = 0;
@@ -936,10 +1013,11 @@ __device__ __noinline__ TrackEval track_offfield(const FieldView& F, bool off, d
 	if (!off) return r;
 	/* f as eval_f_df and w as eval_point_df off the root box, with the
 	   smooth-mass d alpha / d zbar series evaluated once */
-	const double2 ds = smooth_dzbar_any(F, z);
+	const double2 ds = series ? sm.ds : smooth_dzbar_any(F, z);
 	const double a = 1 - F.kappa_tot - smooth_dz(F, z);
 	const double2 f = make_double2(F.shear + F.theta2 * ns.s2.x - ds.x - a * cphi, F.theta2 * ns.s2.y + ds.y + a * sphi);
-	const double2 df = eval_df_mixed(F, -1, z, ns.s3);
+	const double2 df = series ? make_double2(-2 * F.theta2 * ns.s3.x - sm.d2s.x, -2 * F.theta2 * ns.s3.y + sm.d2s.y)
+	                          : eval_df_mixed(F, -1, z, ns.s3);
 	double2 S = make_double2(0, 0);
 	if (disc_exact)
 	{
@@ -959,7 +1037,7 @@ __device__ __noinline__ TrackEval track_offfield(const FieldView& F, bool off, d
 	   tolerance, or a stalled root kept as it is */
 	if (r.as2 < wtol2)
 	{
-		const double2 as = smooth_alpha_any(F, z);
+		const double2 as = series ? sm.alpha : smooth_alpha_any(F, z);
 		const double2 w = make_double2((1 - F.kappa_tot) * z.x + F.shear * z.x - F.theta2 * ns.s1.x - as.x,
 			(1 - F.kappa_tot) * z.y - F.shear * z.y + F.theta2 * ns.s1.y - as.y);
 		r.wpart = dfc_from(w);
