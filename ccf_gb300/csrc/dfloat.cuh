@@ -126,6 +126,28 @@ CCF_D void dfacc_add(dfacc& a, dfl x)
 	a.lo = __fadd_rn(a.lo, __fadd_rn(s.lo, x.lo));
 }
 CCF_D dfl dfacc_get(dfacc a) { return fast_two_sum(a.hi, a.lo); }
+/* a += x y */
+CCF_D void dfacc_fma(dfacc& a, dfl x, dfl y)
+{
+	const float p = __fmul_rn(x.hi, y.hi);
+	const float pe = __fmaf_rn(x.hi, y.hi, -p);
+	const dfl s = two_sum(a.hi, p);
+	a.hi = s.hi;
+	a.lo = __fadd_rn(a.lo, __fadd_rn(s.lo, __fmaf_rn(x.hi, y.lo, __fmaf_rn(x.lo, y.hi, pe))));
+}
+
+/* x^2 + y^2, double-float, one renormalisation (no cancellation: error
+   ~2^-47 of the result) */
+CCF_D dfl df_sumsq(dfl x, dfl y)
+{
+	const float p = __fmul_rn(x.hi, x.hi);
+	const float pe = __fmaf_rn(x.hi, x.hi, -p);
+	const float q = __fmul_rn(y.hi, y.hi);
+	const float qe = __fmaf_rn(y.hi, y.hi, -q);
+	const dfl s = two_sum(p, q);
+	const float lo = __fadd_rn(__fadd_rn(pe, qe), __fmaf_rn(__fmul_rn(2.0f, x.hi), x.lo, __fmaf_rn(__fmul_rn(2.0f, y.hi), y.lo, s.lo)));
+	return fast_two_sum(s.hi, lo);
+}
 
 /* complex */
 CCF_D dfc dfc_from(double2 z) { return {df_from_double(z.x), df_from_double(z.y)}; }
@@ -153,6 +175,20 @@ CCF_D dfl df_dot2_add(dfl x, dfl y, dfl u, dfl z, dfl c)
 	const float e2 = __fmaf_rn(u.lo, z.hi, __fmaf_rn(u.hi, z.lo, qe));
 	const float lo = __fadd_rn(__fadd_rn(e1, e2), __fadd_rn(__fadd_rn(s.lo, t.lo), c.lo));
 	return fast_two_sum(t.hi, lo);
+}
+
+/* x y + u z, real double-float, one renormalisation: error ~2^-47 of
+   |x y| + |u z| */
+CCF_D dfl df_dot2(dfl x, dfl y, dfl u, dfl z)
+{
+	const float p = __fmul_rn(x.hi, y.hi);
+	const float pe = __fmaf_rn(x.hi, y.hi, -p);
+	const float q = __fmul_rn(u.hi, z.hi);
+	const float qe = __fmaf_rn(u.hi, z.hi, -q);
+	const dfl s = two_sum(p, q);
+	const float e1 = __fmaf_rn(x.lo, y.hi, __fmaf_rn(x.hi, y.lo, pe));
+	const float e2 = __fmaf_rn(u.lo, z.hi, __fmaf_rn(u.hi, z.lo, qe));
+	return fast_two_sum(s.hi, __fadd_rn(__fadd_rn(e1, e2), s.lo));
 }
 
 /* a b + c, complex double-float (one Horner step) */

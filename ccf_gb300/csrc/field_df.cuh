@@ -132,7 +132,7 @@ CCF_D double2 smooth_dzbar_df(const FieldView& F, double2 z)
 	const dfc r = dfc_mul(zb, dfc_load(F.inv_corner_df));
 	const dfc u = dfc_mul(r, r);
 	dfc acc = dfc_load(F.smooth_d1_df[F.smooth_m - 1]);
-	for (int m = F.smooth_m - 2; m >= 0; m--) acc = dfc_add(dfc_mul(acc, u), dfc_load(F.smooth_d1_df[m]));
+	for (int m = F.smooth_m - 2; m >= 0; m--) acc = dfc_fma(acc, u, dfc_load(F.smooth_d1_df[m]));
 	acc = dfc_mul(acc, u);
 	double2 d = dfc_to(acc);
 	d.x += F.smooth_k1;
@@ -148,7 +148,7 @@ CCF_D double2 smooth_alpha_df(const FieldView& F, double2 z)
 	const dfc w = dfc_mul(dfc_from(make_double2(z.x, -z.y)), dfc_load(F.inv_corner_df));
 	const int n = F.taylor_smooth + 1;
 	dfc acc = dfc_load(F.smooth_a_df[n]);
-	for (int i = n - 1; i >= 0; i--) acc = dfc_add(dfc_mul(acc, w), dfc_load(F.smooth_a_df[i]));
+	for (int i = n - 1; i >= 0; i--) acc = dfc_fma(acc, w, dfc_load(F.smooth_a_df[i]));
 	double2 a = cmul(dfc_to(acc), make_double2(0, -k / PI));
 	a.x -= k * 2 * (F.corner.x + z.x);
 	return a;
@@ -287,17 +287,17 @@ CCF_D TrackEval eval_track_df(const FieldView& F, const TrackConst& K, int leaf,
 		const dfl m = {mm.x, mm.y};
 		const dfl dx = df_sub(zr.re, s.re);
 		const dfl dy = df_sub(zr.im, s.im);
-		const dfl r = df_rcp(df_add_fast(df_sqr(dx), df_sqr(dy)));
+		const dfl r = df_rcp(df_sumsq(dx, dy));
 		const dfl ix = df_mul(dx, r);
 		const dfl iy = df_neg(df_mul(dy, r));                     /* 1/d */
 		/* ix^2 - iy^2 to 2^-47 of 1/|d|^2, the size of the term */
-		const dfl i2x = df_add_fast(df_sqr(ix), df_neg(df_sqr(iy)));
+		const dfl i2x = df_dot2(ix, ix, df_neg(iy), iy);
 		dfl i2y = df_mul(ix, iy);
 		i2y = {2.f * i2y.hi, 2.f * i2y.lo};                        /* 1/d^2 */
-		dfacc_add(s2r, df_mul(m, i2x));
-		dfacc_add(s2i, df_mul(m, i2y));
-		dfacc_add(s1r, df_mul(m, ix));
-		dfacc_add(s1i, df_mul(m, iy));
+		dfacc_fma(s2r, m, i2x);
+		dfacc_fma(s2i, m, i2y);
+		dfacc_fma(s1r, m, ix);
+		dfacc_fma(s1i, m, iy);
 		pole.x += ix.hi;
 		pole.y += iy.hi;
 		const float i3x = i2x.hi * ix.hi - i2y.hi * iy.hi;
@@ -341,12 +341,12 @@ CCF_D TrackEval eval_track_df(const FieldView& F, const TrackConst& K, int leaf,
 		const dfc wc = dfc_mul(zb, dfc_load(F.inv_corner_df));   /* zbar / c */
 		const dfc u = dfc_mul(wc, wc);
 		dfc acc = dfc_load(F.smooth_d1_df[F.smooth_m - 1]);
-		for (int m = F.smooth_m - 2; m >= 0; m--) acc = dfc_add(dfc_mul(acc, u), dfc_load(F.smooth_d1_df[m]));
+		for (int m = F.smooth_m - 2; m >= 0; m--) acc = dfc_fma(acc, u, dfc_load(F.smooth_d1_df[m]));
 		ds = dfc_mul(acc, u);
 		ds.re = df_add(ds.re, K.k1);
 		const int na = F.taylor_smooth + 1;
 		dfc aa = dfc_load(F.smooth_a_df[na]);
-		for (int i = na - 1; i >= 0; i--) aa = dfc_add(dfc_mul(aa, wc), dfc_load(F.smooth_a_df[i]));
+		for (int i = na - 1; i >= 0; i--) aa = dfc_fma(aa, wc, dfc_load(F.smooth_a_df[i]));
 		/* (0, -k / pi) A: re = (k / pi) A.im, im = -(k / pi) A.re */
 		sa.re = df_mul(K.kpi, aa.im);
 		sa.im = df_neg(df_mul(K.kpi, aa.re));
