@@ -110,8 +110,16 @@ CCF_D void star_term_df(SumsDF& a, dfc& s3, float2& s3f, const dfc& z, float4 p,
 /* Horner of a double-float coefficient block: sum_{i >= first} L[i] dz^(i - first) */
 CCF_D dfc horner_df(const float4* L, int P, int first, dfc dz)
 {
+	/* each coefficient is loaded one step ahead of its use, so the load's
+	   latency overlaps the previous step's arithmetic */
 	dfc acc = dfc_load(L[P]);
-	for (int i = P - 1; i >= first; i--) acc = dfc_fma(acc, dz, dfc_load(L[i]));
+	float4 nxt = L[P - 1];
+	for (int i = P - 1; i >= first; i--)
+	{
+		const float4 cur = nxt;
+		nxt = L[i > 0 ? i - 1 : 0];
+		acc = dfc_fma(acc, dz, dfc_load(cur));
+	}
 	return acc;
 }
 
@@ -280,10 +288,15 @@ CCF_D TrackEval eval_track_df(const FieldView& F, const TrackConst& K, int leaf,
 	const int n = F.leaf_near_count[leaf];
 	const float4* Pn = F.leaf_near_df + (size_t)leaf * MAX_NEAR;
 	const float2* Mn = F.leaf_mass_df + (size_t)leaf * MAX_NEAR;
+	/* the next star is loaded while this one's terms are formed */
+	float4 pn = Pn[0];
+	float2 mn = Mn[0];
 	for (int i = 0; i < n; i++)
 	{
-		const dfc s = dfc_load(Pn[i]);
-		const float2 mm = Mn[i];
+		const dfc s = dfc_load(pn);
+		const float2 mm = mn;
+		pn = Pn[min(i + 1, MAX_NEAR - 1)];
+		mn = Mn[min(i + 1, MAX_NEAR - 1)];
 		const dfl m = {mm.x, mm.y};
 		const dfl dx = df_sub(zr.re, s.re);
 		const dfl dy = df_sub(zr.im, s.im);
@@ -318,8 +331,13 @@ CCF_D TrackEval eval_track_df(const FieldView& F, const TrackConst& K, int leaf,
 	const dfc dl = horner_df(L + (P + 1), P, 2, dz);
 	const float2 dzf = make_float2(dz.re.hi, dz.im.hi);
 	const float2* L3 = (folded ? F.leaf_loc3f_fold : F.leaf_loc3f) + (size_t)leaf * (P + 1);
-	float2 d2l = L3[P];
-	for (int i = P - 1; i >= 3; i--) d2l = fadd(fmulc(d2l, dzf), L3[i]);
+	float2 d2l = L3[P], l3n = L3[P - 1];
+	for (int i = P - 1; i >= 3; i--)
+	{
+		const float2 c = l3n;
+		l3n = L3[i - 1];
+		d2l = fadd(fmulc(d2l, dzf), c);
+	}
 
 	/* smooth mass: d alpha / d zbar (double-float), d2 alpha / d zbar2 (FP32)
 	   and the Taylor part of alpha (double-float) */
