@@ -922,10 +922,12 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		T.items_per_row = 0;
 		T.max_sub = TRACK_TSUB;
 		T.num_items = 0;
+		long long max_row_points = 0;   /* the column check's points of the longest row */
 		for (size_t r = 0; r < rc.size(); r++)
 		{
 			item_start_host[r] = T.num_items;
 			T.num_items += (fields[rc[r].field]->d.num_roots + 31) / 32;
+			max_row_points = std::max(max_row_points, (long long)fields[rc[r].field]->d.num_roots * rc[r].steps);
 		}
 		CCF_TRY(cudaMemcpyAsync(P.item_start.ptr, item_start_host.data(), rc.size() * sizeof(int), cudaMemcpyHostToDevice, s),
 			"upload");
@@ -941,7 +943,7 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		CCF_TRY(cudaMemsetAsync(P.row_stats2.ptr, 0, TRACK_ROW_STATS * rc.size() * sizeof(unsigned long long), s), "memset");
 		CCF_TRY(launch_track_mark(s, T), "track_mark");
 		CCF_TRY(launch_track(s, T, mixed), "track_ccs");
-		CCF_TRY(launch_track_check(s, T, num_sms), "track_check");
+		CCF_TRY(launch_track_check(s, T, max_row_points), "track_check");
 		CCF_TRY(launch_collect_rerun(s, T, P.rows_rerun.ptr, P.rerun_count.ptr), "collect_rerun");
 		/* rows that failed: tracked again from their centre with sub-steps of at
 		   most 1/TRACK_FINE_SUB of a phi step (the predictor's error falls as
@@ -957,7 +959,7 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		T2.counter = P.rerun_count.ptr + 4;
 		CCF_TRY(launch_clear_tables(s, T2), "clear_tables");
 		CCF_TRY(launch_track(s, T2, mixed), "track_ccs_fine");
-		CCF_TRY(launch_track_check(s, T2, num_sms), "track_check");
+		CCF_TRY(launch_track_check(s, T2, max_row_points), "track_check");
 		CCF_TRY(launch_collect_rerun(s, T2, P.rows_rerun2.ptr, P.rerun_count.ptr + 3), "collect_rerun");
 		A.rows = P.rows_rerun2.ptr;
 		A.num_rows_dev = P.rerun_count.ptr + 3;

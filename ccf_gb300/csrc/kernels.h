@@ -295,7 +295,7 @@ cudaError_t launch_solve(cudaStream_t s, const SolveArgs& a, bool mixed, bool in
 cudaError_t launch_track_mark(cudaStream_t s, const TrackArgs& a);
 cudaError_t launch_phase_table(cudaStream_t s, int nb, int nphi, PhaseEntry* out);
 cudaError_t launch_track(cudaStream_t s, const TrackArgs& a, bool mixed);
-cudaError_t launch_track_check(cudaStream_t s, const TrackArgs& a, int num_sms);
+cudaError_t launch_track_check(cudaStream_t s, const TrackArgs& a, long long max_row_points);
 cudaError_t launch_collect_rerun(cudaStream_t s, const TrackArgs& a, RowDesc* rerun, int* count);
 cudaError_t launch_clear_tables(cudaStream_t s, const TrackArgs& a);
 cudaError_t launch_eval_points(cudaStream_t s, const FieldView* F_dev, int npts, const double2* z, const double* phi,

@@ -1622,23 +1622,25 @@ __global__ void clear_tables_kernel(const TrackArgs T)
    cells, and a cell taken twice (two roots of the row converged to one zero)
    flags the row, as the tracker's own insert would.  One thread per stored
    point, the steps of a root in consecutive threads (consecutive columns of
-   the output layout); every block walks the rows in order, so the tables in
-   use at a time stay in L2.  Points whose column the output window does not
-   hold, and fields with outputs in host memory, were checked by the tracker
-   itself.  A lost root leaves stale values in its later columns, which can
-   only flag its own row, already flagged as lost. */
+   the output layout); blockIdx.y is the row, and the blocks of a row are
+   scheduled together, so the tables in use at a time stay in L2.  Points
+   whose column the output window does not hold, and fields with outputs in
+   host memory, were checked by the tracker itself.  A lost root leaves stale
+   values in its later columns, which can only flag its own row, already
+   flagged as lost. */
 __global__ void track_check_kernel(const TrackArgs T)
 {
 	const int nrows = T.num_rows_dev ? *T.num_rows_dev : T.num_rows;
-	for (int q = 0; q < nrows; q++)
+	for (int q = blockIdx.y; q < nrows; q += gridDim.y)
 	{
 		const RowDesc RD = T.rows[q];
-		const FieldOut O = T.outs[RD.field];
+		const FieldOut& O = T.outs[RD.field];
 		if (O.check_inline) continue;
 		const int R = T.fields[RD.field].num_roots;
 		const double inv_cell = CELL_PER_THETA / T.fields[RD.field].theta;
 		const int j0 = O.step_first, nsteps = RD.steps - j0 + 1;
 		if (nsteps <= 0) continue;
+		const int nb = O.nb, half = O.half, seg = O.seg;
 		const unsigned long long slots = 2ull * (unsigned long long)R;
 		const long long n = (long long)R * nsteps;
 		unsigned flags = 0;
@@ -1646,7 +1648,7 @@ __global__ void track_check_kernel(const TrackArgs T)
 		{
 			const int a = (int)(i / nsteps), j = j0 + (int)(i - (long long)a * nsteps);
 			int ob[2], ok[2];
-			row_slots(O.nb, O.half, O.seg, RD.branch, RD.side, j, ob, ok);
+			row_slots(nb, half, seg, RD.branch, RD.side, j, ob, ok);
 			const size_t out = out_slot(O, a, ob[0], ok[0]);
 			if (out == NO_OUT) continue;
 			flags |= (unsigned)table_insert(T.table + RD.cont_base + (size_t)(j - j0) * slots, slots,
@@ -1656,10 +1658,12 @@ __global__ void track_check_kernel(const TrackArgs T)
 	}
 }
 
-cudaError_t launch_track_check(cudaStream_t s, const TrackArgs& a, int num_sms)
+cudaError_t launch_track_check(cudaStream_t s, const TrackArgs& a, long long max_row_points)
 {
-	if (a.num_rows == 0) return cudaSuccess;
-	track_check_kernel<<<num_sms * 8, 256, 0, s>>>(a);
+	if (a.num_rows == 0 || max_row_points <= 0) return cudaSuccess;
+	/* about four points per thread; a row's blocks go out together */
+	const long long gx = std::min<long long>((max_row_points + 1023) / 1024, 1LL << 20);
+	track_check_kernel<<<dim3((unsigned)gx, (unsigned)std::min(a.num_rows, 65535)), 256, 0, s>>>(a);
 	return cudaGetLastError();
 }
 

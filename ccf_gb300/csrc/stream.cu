@@ -439,7 +439,7 @@ ccf_status Engine::solve_chunked(Field& f, int verbose)
 			CCF_TRY_S(cudaMemsetAsync(P.row_stats2.ptr, 0, TRACK_ROW_STATS * grows * sizeof(unsigned long long), s), "memset");
 			CCF_TRY_S(launch_track_mark(s, T), "track_mark");
 			CCF_TRY_S(launch_track(s, T, mixed), "track_ccs");
-			CCF_TRY_S(launch_track_check(s, T, num_sms), "track_check");
+			CCF_TRY_S(launch_track_check(s, T, (long long)R * seg * half), "track_check");
 			CCF_TRY_S(launch_collect_rerun(s, T, P.rows_rerun.ptr, P.rerun_count.ptr), "collect_rerun");
 			TrackArgs T2 = T;
 			T2.rows = P.rows_rerun.ptr;
@@ -451,7 +451,7 @@ ccf_status Engine::solve_chunked(Field& f, int verbose)
 			T2.counter = P.rerun_count.ptr + 4;
 			CCF_TRY_S(launch_clear_tables(s, T2), "clear_tables");
 			CCF_TRY_S(launch_track(s, T2, mixed), "track_ccs_fine");
-			CCF_TRY_S(launch_track_check(s, T2, num_sms), "track_check");
+			CCF_TRY_S(launch_track_check(s, T2, (long long)R * seg * half), "track_check");
 			CCF_TRY_S(launch_collect_rerun(s, T2, P.rows_rerun2.ptr, P.rerun_count.ptr + 3), "collect_rerun");
 			A.rows = P.rows_rerun2.ptr;
 			A.num_rows = grows;
