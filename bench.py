@@ -218,14 +218,15 @@ class ClockSampler:
 
 
 # DRAM bytes (read + write) of the continuation launch per continuation point,
-# from the ncu capture summarised in
-# profiles/track_kernel_n2000_salpeter_phi512.md: 75.2 MB for the 4056 * 512
-# continuation points of that launch (the 40-byte outputs and the column
-# tables; leaf records and stars stay in L2).  It grows with the points written.
-CONT_DRAM_BYTES_PER_POINT = 75.2e6 / (4056 * 512)
-# FP64-pipe activity of the continuation kernel in the same capture
-# (sm__pipe_fp64_cycles_active over active cycles)
-CONT_FP64_PIPE_ACTIVE = 0.350
+# from the full-size one-pass capture summarised in
+# profiles/track_kernel_n2000_salpeter_phi512.md: 35.5 + 172.2 MB for the
+# 4056 * 2048 continuation points of the bench field's launch (the 40-byte
+# outputs, part of which L2 still holds when the launch ends; leaf records
+# and stars stay in L2).
+CONT_DRAM_BYTES_PER_POINT = (35.51e6 + 172.24e6) / (4056 * 2048)
+# FP64-pipe activity of the continuation kernel in the --set full capture of
+# the same profile (sm__pipe_fp64_cycles_active over active cycles)
+CONT_FP64_PIPE_ACTIVE = 0.251
 
 
 def hbm_peak_gbs() -> float | None:
@@ -277,21 +278,22 @@ def continuation_algorithmic_flops(info: dict, approx: int) -> float:
 def tracker_ops_per_eval(info: dict, approx: int) -> float:
     """FP32 operations one tracker evaluation executes (eval_track_df),
     counted from its double-float primitives: two_sum 6, fast_two_sum 3,
-    df_add 20, df_add_fast 11, df_mul 7, df_sqr 7, df_rcp 30; a complex
-    double-float Horner step 81.  Per near star 234 (1/d, 1/d^2, the m/d and
-    m/d^2 sums in double-float, pole and m/d^3 in FP32); the alpha and
-    d alpha/d zbar Horner passes over the local expansion; the FP32 f' pass;
-    for the rectangular Taylor smooth mass the d alpha/d zbar and alpha
-    series, charged to the unfolded share of the leaves; about 200 for the
-    assembly of f, the step and the bookkeeping.  The ratio to
+    df_add 20, df_mul 7, df_sumsq 19, df_dot2 19, df_rcp 13, a running-sum
+    product (dfacc_fma) 12; a complex double-float Horner step (dfc_fma) 54.
+    Per near star 174 (the difference, 1/d, 1/d^2, the m/d and m/d^2 sums in
+    double-float, pole and m/d^3 in FP32); the alpha and d alpha/d zbar
+    Horner passes over the local expansion; the FP32 f' pass; for the
+    rectangular Taylor smooth mass the d alpha/d zbar and alpha series,
+    charged to the unfolded share of the leaves; about 200 for the assembly
+    of f, the step and the bookkeeping.  The ratio to
     algorithmic_flops_per_eval is the cost of the double-float emulation."""
     n = info["near_mean"]
     P = info["expansion_order"]
-    per = 234.0 * n + 81.0 * (2 * P - 3) + 8.0 * max(P - 3, 0) + 200.0
+    per = 174.0 * n + 54.0 * (2 * P - 3) + 8.0 * max(P - 3, 0) + 200.0
     if info["rectangular"] and approx:
         ts = info["taylor_smooth"]
         m = (ts - 1) // 2
-        per += (81.0 * (max(m - 1, 0) + ts + 1) + 8.0 * max(m - 1, 0) + 250.0) * unfolded_share(info)
+        per += (54.0 * (max(m - 1, 0) + ts + 1) + 8.0 * max(m - 1, 0) + 250.0) * unfolded_share(info)
     return per
 
 

@@ -13,7 +13,7 @@ def test_smooth_series_charged_to_unfolded_leaves_only():
     some = bench.tracker_ops_per_eval(dict(HEADLINE_INFO, leaves_folded=1061), approx=1)
     every = bench.tracker_ops_per_eval(dict(HEADLINE_INFO, leaves_folded=1225), approx=1)
     # the base evaluation (near stars, two double-float Horner passes, f' pass, assembly)
-    base = 234.0 * 15.68 + 81.0 * (2 * 23 - 3) + 8.0 * 20 + 200.0
+    base = 174.0 * 15.68 + 54.0 * (2 * 23 - 3) + 8.0 * 20 + 200.0
     assert math.isclose(every, base)
     assert none > some > every
     # the series part scales with the unfolded share of the leaves
