@@ -24,7 +24,8 @@ CLI = os.path.join(LIBDIR, "ccf_gpu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++20", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "-Xcompiler", "-ffp-contract=off", "-I", os.path.join(ROOT, "include")]
-LIB_SOURCES = ["stars.cu", "tree.cu", "fmm.cu", "fmm_check.cu", "solver.cu", "polish.cu", "engine.cu", "stream.cu", "capi.cu",
+LIB_SOURCES = ["stars.cu", "tree.cu", "fmm.cu", "fmm_check.cu", "solver.cu", "polish.cu", "engine.cu", "batch.cu", "stream.cu",
+               "capi.cu",
                "noalloc.cu", "autotune.cpp", "params.cpp", "server.cpp"]
 
 

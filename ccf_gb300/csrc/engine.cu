@@ -33,13 +33,6 @@ The engine never resets the device and reuses its buffers across runs.
 namespace ccf
 {
 
-#define CCF_TRY(expr, what)                              \
-	do                                                   \
-	{                                                    \
-		cudaError_t _e = (expr);                         \
-		if (_e != cudaSuccess) return cuda_fail(_e, what); \
-	} while (0)
-
 Field::~Field()
 {
 	if (events)
@@ -197,7 +190,9 @@ static float ev_ms(cudaEvent_t a, cudaEvent_t b)
 	return ms;
 }
 
-ccf_status Engine::prepare_field(Field& f, int verbose)
+/* parameters, derived values and the star buffers of a field; stars given
+   by the caller or read from a file are uploaded (generation order) */
+ccf_status Engine::setup_begin(Field& f, int verbose)
 {
 	ccf_params& p = f.params;
 	std::string msg;
@@ -254,20 +249,16 @@ ccf_status Engine::prepare_field(Field& f, int verbose)
 		CCF_TRY(cudaMemcpyAsync(f.star_mass.ptr, mass.data(), N * sizeof(double), cudaMemcpyHostToDevice, s), "upload stars");
 		CCF_TRY(cudaStreamSynchronize(s), "upload stars");
 	}
-	else
-	{
-		MassTable mt = make_mass_table(d.mass_kind, d.m_lower, d.m_upper, p.m_solar);
-		launch_generate_stars(s, N, d.random_seed, d.rectangular, make_double2(d.corner_x1, d.corner_x2),
-			std::hypot(d.corner_x1, d.corner_x2), mt, f.star_gen.ptr, f.star_mass.ptr);
-		CCF_TRY(cudaGetLastError(), "generate_stars_kernel");
-	}
-	CCF_TRY(cudaMemcpyAsync(f.star_pos.ptr, f.star_gen.ptr, N * sizeof(double2), cudaMemcpyDeviceToDevice, s), "copy stars");
-	launch_star_stats(s, N, f.star_mass.ptr, f.stats5.ptr);
-	double st[5];
-	CCF_TRY(cudaMemcpyAsync(st, f.stats5.ptr, 5 * sizeof(double), cudaMemcpyDeviceToHost, s), "star stats");
-	CCF_TRY(cudaStreamSynchronize(s), "star stats");
+	return CCF_OK;
+}
 
-	/* include/star.cuh:124-161 and include/ccf.cuh:676-700 */
+/* the field's info from its star statistics (include/star.cuh:124-161 and
+   include/ccf.cuh:676-700), and the corner from the actual mean mass */
+void Engine::setup_stats(Field& f, const double* st)
+{
+	ccf_params& p = f.params;
+	Derived& d = f.d;
+	const int N = d.num_stars;
 	ccf_info& info = f.info;
 	std::memset(&info, 0, sizeof(info));
 	info.m_lower_actual = st[3];
@@ -282,17 +273,51 @@ ccf_status Engine::prepare_field(Field& f, int verbose)
 		info.kappa_star_actual = st[0] * d.theta * d.theta / (a * a);
 	}
 	update_corner(p, d, info.mean_mass_actual);
+}
+
+ccf_status Engine::prepare_field(Field& f, int verbose)
+{
+	ccf_status rc = setup_begin(f, verbose);
+	if (rc != CCF_OK) return rc;
+	ccf_params& p = f.params;
+	Derived& d = f.d;
+	const int N = d.num_stars;
+	cudaStream_t s = stream;
+	if (!d.star_input)
+	{
+		MassTable mt = make_mass_table(d.mass_kind, d.m_lower, d.m_upper, p.m_solar);
+		launch_generate_stars(s, N, d.random_seed, d.rectangular, make_double2(d.corner_x1, d.corner_x2),
+			std::hypot(d.corner_x1, d.corner_x2), mt, f.star_gen.ptr, f.star_mass.ptr);
+		CCF_TRY(cudaGetLastError(), "generate_stars_kernel");
+	}
+	CCF_TRY(cudaMemcpyAsync(f.star_pos.ptr, f.star_gen.ptr, N * sizeof(double2), cudaMemcpyDeviceToDevice, s), "copy stars");
+	launch_star_stats(s, N, f.star_mass.ptr, f.stats5.ptr);
+	double st[5];
+	CCF_TRY(cudaMemcpyAsync(st, f.stats5.ptr, 5 * sizeof(double), cudaMemcpyDeviceToHost, s), "star stats");
+	CCF_TRY(cudaStreamSynchronize(s), "star stats");
+	setup_stats(f, st);
 	CCF_TRY(cudaEventRecord(f.ev[1], s), "event");
 	if (verbose >= 1) std::cout << "Done generating star field.\n";
 
 	if (verbose >= 1) std::cout << "Creating children and sorting stars...\n";
-	ccf_status rc = build_tree(f);
+	rc = build_tree(f);
 	if (rc != CCF_OK) return rc;
 	rc = build_fmm(f);
 	if (rc != CCF_OK) return rc;
 	CCF_TRY(cudaEventRecord(f.ev[2], s), "event");
 	if (verbose >= 1) std::cout << "Done calculating multipole and local coefficients.\n";
+	return setup_outputs(f);
+}
 
+/* output buffers (device, or page-locked host memory with host_outputs),
+   the solver statistics and the rest of the field's info */
+ccf_status Engine::setup_outputs(Field& f)
+{
+	ccf_params& p = f.params;
+	Derived& d = f.d;
+	ccf_info& info = f.info;
+	const int N = d.num_stars;
+	cudaStream_t s = stream;
 	/* outputs */
 	const int R = d.num_roots, nb = p.num_branches, cols = p.num_phi / nb + 1;
 	const size_t npts = (size_t)R * nb * cols;
@@ -364,15 +389,11 @@ ccf_status Engine::prepare_field(Field& f, int verbose)
 	return CCF_OK;
 }
 
-ccf_status Engine::build_tree(Field& f)
+/* node arrays for cap nodes, the first keep of them kept */
+cudaError_t Engine::tree_capacity(Field& f, int cap, int keep)
 {
 	cudaStream_t s = stream;
-	const int N = f.d.num_stars;
-	double rhl = f.d.rectangular ? std::max(f.d.corner_x1, f.d.corner_x2) : std::hypot(f.d.corner_x1, f.d.corner_x2);
-	rhl = rhl * 1.1;   /* include/ccf.cuh:746 */
-	f.info.root_half_length = rhl;
-
-	auto alloc_nodes = [&](int cap, int keep) -> cudaError_t {
+	{
 		cudaError_t e;
 		if ((e = f.n_center.grow(cap, keep, s)) != cudaSuccess) return e;
 		if ((e = f.n_half.grow(cap, keep, s)) != cudaSuccess) return e;
@@ -391,7 +412,16 @@ ccf_status Engine::build_tree(Field& f)
 		if ((e = f.n_rank.grow(cap, keep, s)) != cudaSuccess) return e;
 		f.node_cap = cap;
 		return cudaSuccess;
-	};
+	}
+}
+
+ccf_status Engine::build_tree(Field& f)
+{
+	cudaStream_t s = stream;
+	const int N = f.d.num_stars;
+	const double rhl = root_half_length(f.d);
+	f.info.root_half_length = rhl;
+	auto alloc_nodes = [&](int cap, int keep) -> cudaError_t { return tree_capacity(f, cap, keep); };
 	int cap = std::max(1024, 2 * N + 64);
 	if (f.node_cap < cap) CCF_TRY(alloc_nodes(cap, 0), "cudaMalloc(tree)");
 	CCF_TRY(f.level_out.ensure(4), "cudaMalloc(tree)");
@@ -399,9 +429,8 @@ ccf_status Engine::build_tree(Field& f)
 	f.level_count.assign(1, 1);
 	launch_tree_root(s, f.tree_dev(), rhl, N);
 	CCF_TRY(cudaMemsetAsync(f.level_out.ptr, 0, 4 * sizeof(int), s), "memset");
-	/* a node splits while its stars and its neighbours' exceed the leaf limit
-	   (the reference's 32 unless leaf_max_stars lowers it) */
-	const int limit = f.params.leaf_max_stars > 0 ? std::min(f.params.leaf_max_stars, MAX_NEAR) : MAX_NEAR;
+	/* a node splits while its stars and its neighbours' exceed the leaf limit */
+	const int limit = leaf_limit(f.params);
 	int L = 0;
 	while (true)
 	{
@@ -433,18 +462,26 @@ ccf_status Engine::build_tree(Field& f)
 	return CCF_OK;
 }
 
+/* the expansion order (include/ccf.cuh:840-852), or the explicit one */
+ccf_status Engine::fmm_order(Field& f, int levels, int& P)
+{
+	const Derived& d = f.d;
+	P = (int)std::ceil(2 * std::log2(d.theta) + levels - std::log2(f.info.root_half_length) - std::log2(d.alpha_error));
+	if (f.params.expansion_order > 0) P = f.params.expansion_order;   /* validated in [3, MAX_ORDER] */
+	if (P < 3) { error = "Error. Expansion order needs to be >= 3"; return CCF_ERR_INVALID_ARGUMENT; }
+	if (P > MAX_ORDER) { error = "Error. Maximum allowed expansion order is " + std::to_string(MAX_ORDER); return CCF_ERR_INVALID_ARGUMENT; }
+	return CCF_OK;
+}
+
 ccf_status Engine::build_fmm(Field& f)
 {
 	cudaStream_t s = stream;
 	ccf_params& p = f.params;
 	Derived& d = f.d;
 	const int levels = (int)f.level_start.size() - 1;
-	const double rhl = f.info.root_half_length;
-	/* include/ccf.cuh:840-852 */
-	int P = (int)std::ceil(2 * std::log2(d.theta) + levels - std::log2(rhl) - std::log2(d.alpha_error));
-	if (p.expansion_order > 0) P = p.expansion_order;   /* an explicit order (validated in [3, MAX_ORDER]) */
-	if (P < 3) { error = "Error. Expansion order needs to be >= 3"; return CCF_ERR_INVALID_ARGUMENT; }
-	if (P > MAX_ORDER) { error = "Error. Maximum allowed expansion order is " + std::to_string(MAX_ORDER); return CCF_ERR_INVALID_ARGUMENT; }
+	int P = 0;
+	ccf_status rc = fmm_order(f, levels, P);
+	if (rc != CCF_OK) return rc;
 	std::vector<double> B = binomial_table(2 * P, !p.exact_binomials);
 	CCF_TRY(f.binom.ensure(B.size()), "cudaMalloc(binomials)");
 	CCF_TRY(cudaMemcpyAsync(f.binom.ptr, B.data(), B.size() * sizeof(double), cudaMemcpyHostToDevice, s), "binomials");
@@ -506,14 +543,30 @@ ccf_status Engine::build_fmm(Field& f)
 
 	/* mean near-list length over the leaves (reported; the tracker's work per
 	   evaluation grows with it) */
+	double near_sum = 0;
 	{
 		std::vector<int> cnt(nl);
 		CCF_TRY(cudaMemcpyAsync(cnt.data(), f.leaf_near_count.ptr, nl * sizeof(int), cudaMemcpyDeviceToHost, s), "near counts");
 		CCF_TRY(cudaStreamSynchronize(s), "near counts");
-		double sum = 0;
-		for (int v : cnt) sum += v;
-		f.info.near_mean = nl > 0 ? sum / nl : 0;
+		for (int v : cnt) near_sum += v;
 	}
+	int lerr = 0;
+	CCF_TRY(cudaMemcpyAsync(&lerr, f.level_out.ptr + 2, sizeof(int), cudaMemcpyDeviceToHost, s), "leaves");
+	CCF_TRY(cudaStreamSynchronize(s), "leaves");
+	return finish_view(f, P, near_sum, lerr);
+}
+
+/* the smooth-mass polynomials, the fold of their series into the leaf
+   expansions (rectangular Taylor form, mixed precision) and the field's
+   device view, after the leaf records */
+ccf_status Engine::finish_view(Field& f, int P, double near_sum, int lerr)
+{
+	cudaStream_t s = stream;
+	ccf_params& p = f.params;
+	Derived& d = f.d;
+	const int nl = f.num_leaves;
+	f.info.near_mean = nl > 0 ? near_sum / nl : 0;
+	if (lerr) { error = "Error. A leaf has more than 32 near stars."; return CCF_ERR_NUMERIC; }
 
 	/* smooth-mass polynomials */
 	float4 inv_corner_df = make_float4(0, 0, 0, 0);
@@ -604,13 +657,9 @@ ccf_status Engine::build_fmm(Field& f)
 			fold_host.resize(nl);
 			CCF_TRY(cudaMemcpyAsync(fold_host.data(), f.leaf_fold.ptr, nl, cudaMemcpyDeviceToHost, s), "fold");
 		}
-		CCF_TRY(cudaStreamSynchronize(s), "smooth");
+		if (fold_ok) CCF_TRY(cudaStreamSynchronize(s), "smooth");
 		for (unsigned char v : fold_host) f.info.leaves_folded += v ? 1 : 0;
 	}
-	int lerr = 0;
-	CCF_TRY(cudaMemcpyAsync(&lerr, f.level_out.ptr + 2, sizeof(int), cudaMemcpyDeviceToHost, s), "leaves");
-	CCF_TRY(cudaStreamSynchronize(s), "leaves");
-	if (lerr) { error = "Error. A leaf has more than 32 near stars."; return CCF_ERR_NUMERIC; }
 
 	FieldView& V = f.view;
 	std::memset(&V, 0, sizeof(V));
@@ -999,10 +1048,11 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 	/* root seeds, initial solve, continuation (tracker: phase table, item
 	   marking, tracking, column check, row collection, table clearing,
 	   re-tracking, column check, row collection and the full-sum launch for
-	   the rows to re-run), FP64 polish */
+	   the rows to re-run), FP64 polish; the launches are shared by the
+	   batch's fields and counted with the first */
 	for (int fi = 0; fi < nf; fi++)
 	{
-		ccf_status rc = finish_stats(*fields[fi], seg[fi], track, verbose, track ? 14 : 5);
+		ccf_status rc = finish_stats(*fields[fi], seg[fi], track, verbose, fi > 0 ? 0 : track ? 14 : 5);
 		if (rc != CCF_OK) status = rc;
 	}
 	return status;
@@ -1087,7 +1137,28 @@ static int setup_threads()
 	return n;
 }
 
+bool batch_setup_fits(const Field& f);   /* batch.cu */
+
 ccf_status Engine::prepare_fields(std::vector<Field*>& fields, int verbose)
+{
+	/* a batch of small fields is set up by the batched launches (batch.cu);
+	   the others one by one, on setup threads when there are many */
+	if (fields.size() >= 2)
+	{
+		std::vector<Field*> small, rest;
+		for (Field* f : fields) (batch_setup_fits(*f) ? small : rest).push_back(f);
+		if (small.size() >= 2)
+		{
+			ccf_status rc = prepare_batch(small, verbose);
+			if (rc != CCF_OK) return rc;
+			if (rest.empty()) return CCF_OK;
+			return prepare_fields_each(rest, verbose);
+		}
+	}
+	return prepare_fields_each(fields, verbose);
+}
+
+ccf_status Engine::prepare_fields_each(std::vector<Field*>& fields, int verbose)
 {
 	const int nf = (int)fields.size();
 	const int T = nf >= SETUP_PARALLEL_MIN ? std::min(setup_threads(), nf) : 1;

@@ -215,6 +215,27 @@ struct SolverPools
 	DBuf<int> error;
 };
 
+/* inside an Engine member returning ccf_status: a CUDA error becomes the
+   engine's error message and CCF_ERR_CUDA */
+#define CCF_TRY(expr, what)                              \
+	do                                                   \
+	{                                                    \
+		cudaError_t _e = (expr);                         \
+		if (_e != cudaSuccess) return cuda_fail(_e, what); \
+	} while (0)
+
+/* the root's half length (include/ccf.cuh:746) and the leaf limit: the
+   reference's 32 unless leaf_max_stars lowers it */
+inline double root_half_length(const Derived& d)
+{
+	const double rhl = d.rectangular ? std::max(d.corner_x1, d.corner_x2) : std::hypot(d.corner_x1, d.corner_x2);
+	return rhl * 1.1;
+}
+inline int leaf_limit(const ccf_params& p)
+{
+	return p.leaf_max_stars > 0 ? std::min(p.leaf_max_stars, MAX_NEAR) : MAX_NEAR;
+}
+
 class Engine
 {
 public:
@@ -234,9 +255,17 @@ public:
 
 private:
 	ccf_status prepare_fields(std::vector<Field*>& fields, int verbose);
+	ccf_status prepare_fields_each(std::vector<Field*>& fields, int verbose);
 	ccf_status prepare_field(Field& f, int verbose);
 	ccf_status build_tree(Field& f);
 	ccf_status build_fmm(Field& f);
+	cudaError_t tree_capacity(Field& f, int cap, int keep);
+	ccf_status fmm_order(Field& f, int levels, int& P);
+	ccf_status setup_begin(Field& f, int verbose);
+	void setup_stats(Field& f, const double* st);
+	ccf_status finish_view(Field& f, int P, double near_sum, int lerr);
+	ccf_status setup_outputs(Field& f);
+	ccf_status prepare_batch(std::vector<Field*>& fields, int verbose);
 	ccf_status solve(std::vector<Field*>& fields, int verbose);
 	ccf_status solve_chunked(Field& f, int verbose);   /* stream.cu */
 	int solved_seg(const Field& f, bool track) const;
@@ -262,6 +291,10 @@ private:
 		cudaStream_t copy = nullptr;
 		cudaEvent_t ready = nullptr, copied[2] = {nullptr, nullptr}, done = nullptr;
 	} chunk;
+	/* batched setup: the fields' descriptors and their info words */
+	DBuf<BatchSeg> batch_segs;
+	DBuf<int> batch_info;
+	DBuf<double> batch_stats;
 	/* batch setup: engines (their streams) of the setup threads, and events */
 	std::vector<std::unique_ptr<Engine>> setup_workers;
 	std::vector<cudaEvent_t> setup_events;

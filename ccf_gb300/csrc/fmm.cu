@@ -47,13 +47,9 @@ CCF_D double2 shfl_c(double2 v, int src)
 /* upward pass at one level: P2M for leaves holding stars, M2M for split
    nodes.  The stars of a leaf are taken 32 at a time, one per lane, and
    handed round the warp by shuffles; the powers come from warp_powers. */
-__global__ void fmm_upward_kernel(TreeDev T, int start, int count, int P, const double2* __restrict__ pos,
+CCF_D void fmm_upward_node(const TreeDev& T, int n, int P, int p, const double2* __restrict__ pos,
 	const double* __restrict__ mass, double2* __restrict__ multi, const double* __restrict__ B)
 {
-	int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-	int p = threadIdx.x & 31;
-	if (w >= count) return;   /* warp-uniform */
-	int n = start + w;
 	const bool act = p <= P;
 	double2 r = make_double2(0, 0);
 	int ch = T.child[n];
@@ -125,6 +121,14 @@ __global__ void fmm_upward_kernel(TreeDev T, int start, int count, int P, const 
 	if (act) multi[(size_t)n * (P + 1) + p] = r;
 }
 
+__global__ void fmm_upward_kernel(TreeDev T, int start, int count, int P, const double2* __restrict__ pos,
+	const double* __restrict__ mass, double2* __restrict__ multi, const double* __restrict__ B)
+{
+	int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	if (w >= count) return;   /* warp-uniform */
+	fmm_upward_node(T, start + w, P, threadIdx.x & 31, pos, mass, multi, B);
+}
+
 /* downward pass at one level >= 2: L2L from the parent, then M2L from the
    same-level interaction list, then P2L from the coarser-leaf list, summed
    in that order (include/ccf.cuh:880-893).  GB300's FP64 pipe is 1/64 of its
@@ -134,14 +138,10 @@ __global__ void fmm_upward_kernel(TreeDev T, int start, int count, int P, const 
    handed round by shuffles; lane p takes t^p from a product scan; and the
    M2L sum over k is a binomial-weighted sum of the pre-scaled b_k t^k (two
    FMAs a term) instead of a complex Horner recurrence. */
-__global__ void fmm_downward_kernel(TreeDev T, int start, int count, int P, const double2* __restrict__ pos,
+CCF_D void fmm_downward_node(const TreeDev& T, int n, int P, int p, const double2* __restrict__ pos,
 	const double* __restrict__ mass, const double2* __restrict__ multi, double2* __restrict__ local,
 	const double* __restrict__ B)
 {
-	int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-	int p = threadIdx.x & 31;
-	if (w >= count) return;   /* warp-uniform */
-	int n = start + w;
 	const bool act = p <= P;
 	double2 cn = T.center[n];
 	double2 r = make_double2(0, 0);
@@ -252,21 +252,26 @@ __global__ void fmm_downward_kernel(TreeDev T, int start, int count, int P, cons
 	if (act) local[(size_t)n * (P + 1) + p] = r;
 }
 
+__global__ void fmm_downward_kernel(TreeDev T, int start, int count, int P, const double2* __restrict__ pos,
+	const double* __restrict__ mass, const double2* __restrict__ multi, double2* __restrict__ local,
+	const double* __restrict__ B)
+{
+	int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	if (w >= count) return;   /* warp-uniform */
+	fmm_downward_node(T, start + w, P, threadIdx.x & 31, pos, mass, multi, local, B);
+}
+
 /* leaf records for the solver: centre, 1/h, packed near stars (neighbours
    first, then the leaf's own stars, as include/alpha_star.cuh:26-37 sums
    them) and the local coefficients pre-scaled for alpha, d/dzbar, d2/dzbar2:
    L1_i = theta^2 i c_i / h, L2_i = theta^2 i (i-1) c_i / h^2,
    L3_i = theta^2 i (i-1) (i-2) c_i / h^3 */
-__global__ void leaf_build_kernel(TreeDev T, int num_nodes, const int* __restrict__ leaf_index, int P, double theta2,
+CCF_D void leaf_build_node(const TreeDev& T, int n, int lane, const int* __restrict__ leaf_index, int P, double theta2,
 	const double2* __restrict__ pos, const double* __restrict__ mass, const double2* __restrict__ local,
 	double2* __restrict__ leaf_center, double* __restrict__ leaf_inv_half, int* __restrict__ leaf_near_count,
 	NearStar* __restrict__ leaf_near, double2* __restrict__ leaf_loc, float2* __restrict__ leaf_loc3f,
 	int* __restrict__ node_leaf, int* err)
 {
-	int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-	int lane = threadIdx.x & 31;
-	if (w >= num_nodes) return;
-	int n = w;
 	if (T.child[n] >= 0) return;
 	int l = leaf_index[n];
 	if (lane == 0)
@@ -318,6 +323,18 @@ __global__ void leaf_build_kernel(TreeDev T, int num_nodes, const int* __restric
 	}
 }
 
+__global__ void leaf_build_kernel(TreeDev T, int num_nodes, const int* __restrict__ leaf_index, int P, double theta2,
+	const double2* __restrict__ pos, const double* __restrict__ mass, const double2* __restrict__ local,
+	double2* __restrict__ leaf_center, double* __restrict__ leaf_inv_half, int* __restrict__ leaf_near_count,
+	NearStar* __restrict__ leaf_near, double2* __restrict__ leaf_loc, float2* __restrict__ leaf_loc3f,
+	int* __restrict__ node_leaf, int* err)
+{
+	int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	if (w >= num_nodes) return;
+	leaf_build_node(T, w, threadIdx.x & 31, leaf_index, P, theta2, pos, mass, local, leaf_center, leaf_inv_half,
+		leaf_near_count, leaf_near, leaf_loc, leaf_loc3f, node_leaf, err);
+}
+
 void launch_fmm_upward(cudaStream_t s, const TreeDev& T, int start, int count, int P, const double2* pos, const double* mass,
 	double2* multi, const double* B)
 {
@@ -348,14 +365,11 @@ namespace ccf
    near stars relative to the leaf centre (formed in FP64, then split),
    masses, the alpha and d/dzbar coefficient blocks, and 1/h.  One warp per
    leaf. */
-__global__ void leaf_df_kernel(int num_leaves, int P, const double2* __restrict__ leaf_center,
+CCF_D void leaf_df_leaf(int l, int i, int P, const double2* __restrict__ leaf_center,
 	const double* __restrict__ leaf_inv_half, const int* __restrict__ near_count, const NearStar* __restrict__ near,
 	const double2* __restrict__ loc, float4* __restrict__ near_df, float2* __restrict__ mass_df, float4* __restrict__ loc_df,
 	float2* __restrict__ ih_df)
 {
-	const int l = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-	const int i = threadIdx.x & 31;
-	if (l >= num_leaves) return;
 	const double2 c = leaf_center[l];
 	auto split = [](double x) {
 		float h = __double2float_rn(x);
@@ -378,6 +392,16 @@ __global__ void leaf_df_kernel(int num_leaves, int P, const double2* __restrict_
 		}
 	}
 	if (i == 0) ih_df[l] = split(leaf_inv_half[l]);
+}
+
+__global__ void leaf_df_kernel(int num_leaves, int P, const double2* __restrict__ leaf_center,
+	const double* __restrict__ leaf_inv_half, const int* __restrict__ near_count, const NearStar* __restrict__ near,
+	const double2* __restrict__ loc, float4* __restrict__ near_df, float2* __restrict__ mass_df, float4* __restrict__ loc_df,
+	float2* __restrict__ ih_df)
+{
+	const int l = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+	if (l >= num_leaves) return;
+	leaf_df_leaf(l, threadIdx.x & 31, P, leaf_center, leaf_inv_half, near_count, near, loc, near_df, mass_df, loc_df, ih_df);
 }
 
 void launch_leaf_df(cudaStream_t s, int num_leaves, int P, const double2* leaf_center, const double* leaf_inv_half,
@@ -512,6 +536,103 @@ void launch_fold_smooth(cudaStream_t s, int num_leaves, int P, const double2* le
 	const int warps = 4;
 	fold_smooth_kernel<<<(num_leaves + warps - 1) / warps, warps * 32, 0, s>>>(num_leaves, P, leaf_center, leaf_inv_half, loc, ef, nf, er,
 		nr, eq, nq, radius, loc_df, loc3f, loc64, fold);
+}
+
+} /* namespace ccf */
+
+namespace ccf
+{
+
+/* The FMM passes of one field per CTA, for batches: the upward pass level
+   by level from the leaves, the downward pass from level 2, then the leaf
+   numbering -- the node functions of the per-level launches, with block
+   barriers between levels.  The leaf count goes to seg.info for the host. */
+__global__ void __launch_bounds__(512) fmm_batch_kernel(const BatchSeg* __restrict__ segs)
+{
+	const BatchSeg& S = segs[blockIdx.x];
+	const TreeDev T = S.T;
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+	const int levels = S.info[0], nodes = S.info[1], P = S.P;
+	const int* lstart = S.info + 3;
+	const int* lcount = S.info + 3 + TREE_MAX_LEVELS + 1;
+	const size_t nc = (size_t)nodes * (P + 1);
+	for (size_t i = tid; i < nc; i += blockDim.x)
+	{
+		S.multi[i] = make_double2(0, 0);
+		S.local[i] = make_double2(0, 0);
+	}
+	__syncthreads();
+	for (int L = levels; L >= 0; L--)
+	{
+		const int st = lstart[L], cnt = lcount[L];
+		for (int w = warp; w < cnt; w += nw) fmm_upward_node(T, st + w, P, lane, S.pos, S.mass, S.multi, S.B);
+		__syncthreads();
+	}
+	for (int L = 2; L <= levels; L++)
+	{
+		const int st = lstart[L], cnt = lcount[L];
+		for (int w = warp; w < cnt; w += nw) fmm_downward_node(T, st + w, P, lane, S.pos, S.mass, S.multi, S.local, S.B);
+		__syncthreads();
+	}
+	for (int i = tid; i < nodes; i += blockDim.x) S.leaf_flag[i] = T.child[i] < 0;
+	__syncthreads();
+	const int nl = block_exclusive_scan(S.leaf_flag, S.leaf_index, nodes);
+	if (tid == 0) S.info[LEAF_INFO] = nl;
+}
+
+/* The leaf records of one field per CTA, for batches: leaf_build_kernel,
+   leaf_df_kernel and star_hilo_kernel for one field, and the sum of the
+   near-list lengths and the error bits for the host. */
+__global__ void __launch_bounds__(512) leaf_batch_kernel(const BatchSeg* __restrict__ segs)
+{
+	__shared__ int s_err, s_near;
+	const BatchSeg& S = segs[blockIdx.x];
+	const TreeDev T = S.T;
+	const unsigned full = 0xffffffffu;
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+	const int nodes = S.info[1], nl = S.num_leaves;
+	if (tid == 0)
+	{
+		s_err = 0;
+		s_near = 0;
+	}
+	__syncthreads();
+	for (int w = warp; w < nodes; w += nw)
+		leaf_build_node(T, w, lane, S.leaf_index, S.P, S.theta2, S.pos, S.mass, S.local, S.leaf_center, S.leaf_inv_half,
+			S.leaf_near_count, S.leaf_near, S.leaf_loc, S.leaf_loc3f, S.node_leaf, &s_err);
+	__syncthreads();
+	int cnt = 0;
+	for (int l = tid; l < nl; l += blockDim.x) cnt += S.leaf_near_count[l];
+	cnt = __reduce_add_sync(full, cnt);
+	if (lane == 0) atomicAdd(&s_near, cnt);
+	if (S.leaf_near_df)
+	{
+		for (int l = warp; l < nl; l += nw)
+			leaf_df_leaf(l, lane, S.P, S.leaf_center, S.leaf_inv_half, S.leaf_near_count, S.leaf_near, S.leaf_loc,
+				S.leaf_near_df, S.leaf_mass_df, S.leaf_loc_df, S.leaf_ih_df);
+		for (int i = tid; i < S.n; i += blockDim.x)
+		{
+			S.star_hilo[i] = split_hilo(S.pos[i]);
+			const double m = S.mass[i];
+			const float h = __double2float_rn(m);
+			S.star_mass_df[i] = make_float2(h, __double2float_rn(m - (double)h));
+		}
+	}
+	__syncthreads();
+	if (tid == 0)
+	{
+		S.info[LEAF_INFO + 1] = s_near;
+		S.info[LEAF_INFO + 2] = s_err;
+	}
+}
+
+void launch_fmm_batch(cudaStream_t s, const BatchSeg* segs, int nseg)
+{
+	if (nseg > 0) fmm_batch_kernel<<<nseg, 512, 0, s>>>(segs);
+}
+void launch_leaf_batch(cudaStream_t s, const BatchSeg* segs, int nseg)
+{
+	if (nseg > 0) leaf_batch_kernel<<<nseg, 512, 0, s>>>(segs);
 }
 
 } /* namespace ccf */

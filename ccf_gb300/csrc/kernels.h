@@ -263,7 +263,111 @@ void launch_seed_roots(cudaStream_t s, int nstars, int nroots, int nrows, const 
 void launch_star_hilo(cudaStream_t s, int n, const double2* pos, float4* out, const double* mass = nullptr,
 	float2* mass_out = nullptr);
 
+/* One field of a batched setup (tree.cu tree_batch_kernel, fmm.cu
+   fmm_batch_kernel and leaf_batch_kernel, stars.cu stars_batch_kernel): one
+   CTA per field does what the per-level launches do for one field. */
+constexpr int TREE_MAX_LEVELS = 40;
+constexpr int BATCH_INFO_INTS = 3 + 2 * (TREE_MAX_LEVELS + 1) + 4;   /* tree info, then the leaf info */
+struct BatchSeg
+{
+	/* stars (generated when gen is set) */
+	int n;
+	int gen;
+	int seed;
+	int rectangular;
+	double2 corner;
+	double corner_abs;
+	MassTable mt;
+	double2* star_gen;
+	double2* pos;
+	double* mass;
+	double2* tpos;
+	double* tmass;
+	double* stats5;
+	/* tree */
+	TreeDev T;
+	int node_cap;
+	int limit;
+	double root_half;
+	/* info: [0] levels, [1] nodes, [2] error bits (1 a neighbour list overflowed, 2 the node
+	   capacity ran out), [3 ..] level starts, [3 + TREE_MAX_LEVELS + 1 ..] level counts,
+	   then [LEAF_INFO + 0] leaves, [+1] the sum of the near-list lengths, [+2] error bits
+	   (2 a leaf has more than MAX_NEAR near stars) */
+	int* info;
+	/* FMM */
+	int P;
+	const double* B;
+	double2* multi;
+	double2* local;
+	int* leaf_flag;
+	int* leaf_index;
+	/* leaf records */
+	double theta2;
+	int num_leaves;
+	double2* leaf_center;
+	double* leaf_inv_half;
+	int* leaf_near_count;
+	NearStar* leaf_near;
+	double2* leaf_loc;
+	float2* leaf_loc3f;
+	int* node_leaf;
+	float4* leaf_near_df;   /* null: no double-float copies (FP64 precision) */
+	float2* leaf_mass_df;
+	float4* leaf_loc_df;
+	float2* leaf_ih_df;
+	float4* star_hilo;
+	float2* star_mass_df;
+};
+constexpr int LEAF_INFO = 3 + 2 * (TREE_MAX_LEVELS + 1);
+
+/* exclusive scan of n ints by the calling block (every thread calls it;
+   n up to a few million); returns the total */
+CCF_D int block_exclusive_scan(const int* __restrict__ in, int* __restrict__ out, int n)
+{
+	__shared__ int s_warp[32];
+	__shared__ int s_carry;
+	if (threadIdx.x == 0) s_carry = 0;
+	__syncthreads();
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	for (int base = 0; base < n; base += blockDim.x)
+	{
+		int i = base + threadIdx.x;
+		int v = i < n ? in[i] : 0;
+		int x = v;
+		for (int o = 1; o < 32; o <<= 1)
+		{
+			int y = __shfl_up_sync(0xffffffffu, x, o);
+			if (lane >= o) x += y;
+		}
+		if (lane == 31) s_warp[warp] = x;
+		__syncthreads();
+		if (warp == 0)
+		{
+			int w = lane < (int)(blockDim.x >> 5) ? s_warp[lane] : 0;
+			for (int o = 1; o < 32; o <<= 1)
+			{
+				int y = __shfl_up_sync(0xffffffffu, w, o);
+				if (lane >= o) w += y;
+			}
+			s_warp[lane] = w;
+		}
+		__syncthreads();
+		int prefix = s_carry + (warp > 0 ? s_warp[warp - 1] : 0) + x - v;
+		if (i < n) out[i] = prefix;
+		__syncthreads();
+		if (threadIdx.x == blockDim.x - 1) s_carry = prefix + v;
+		__syncthreads();
+	}
+	const int total = s_carry;
+	__syncthreads();
+	return total;
+}
+
+
+void launch_stars_batch(cudaStream_t s, const BatchSeg* segs, int nseg);
+
 /* tree.cu */
+void launch_tree_batch(cudaStream_t s, const BatchSeg* segs, int nseg);
 void launch_tree_root(cudaStream_t s, const TreeDev& T, double half, int nstars);
 void launch_tree_flag(cudaStream_t s, const TreeDev& T, int start, int count, int limit, int* out);
 void launch_scan(cudaStream_t s, const int* in, int* out, int n);
@@ -274,6 +378,8 @@ void launch_tree_neighbors(cudaStream_t s, const TreeDev& T, int start, int coun
 void launch_leaf_flag(cudaStream_t s, const TreeDev& T, int num_nodes, int* flag);
 
 /* fmm.cu */
+void launch_fmm_batch(cudaStream_t s, const BatchSeg* segs, int nseg);
+void launch_leaf_batch(cudaStream_t s, const BatchSeg* segs, int nseg);
 void launch_fmm_upward(cudaStream_t s, const TreeDev& T, int start, int count, int P, const double2* pos, const double* mass,
 	double2* multi, const double* B);
 void launch_fmm_downward(cudaStream_t s, const TreeDev& T, int start, int count, int P, const double2* pos, const double* mass,

@@ -15,11 +15,9 @@ is written back.
 namespace ccf
 {
 
-__global__ void __launch_bounds__(256) generate_stars_kernel(int n, int seed, int rectangular, double2 corner, double corner_abs,
-	MassTable mt, double2* __restrict__ pos, double* __restrict__ mass)
+CCF_D void generate_star(int i, int seed, int rectangular, double2 corner, double corner_abs, const MassTable& mt,
+	double2* __restrict__ pos, double* __restrict__ mass)
 {
-	int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= n) return;
 	curandStateXORWOW_t st;
 	curand_init(seed, i, 0, &st);
 	double x1, x2;
@@ -41,9 +39,17 @@ __global__ void __launch_bounds__(256) generate_stars_kernel(int n, int seed, in
 	mass[i] = mass_draw(mt, curand_uniform_double(&st));
 }
 
-/* Deterministic single-block reduction of the star statistics of
-   include/star.cuh:124-161: total mass, sum m^2, sum m^2 ln m, min, max. */
-__global__ void __launch_bounds__(1024) star_stats_kernel(int n, const double* __restrict__ mass, double* out)
+__global__ void __launch_bounds__(256) generate_stars_kernel(int n, int seed, int rectangular, double2 corner, double corner_abs,
+	MassTable mt, double2* __restrict__ pos, double* __restrict__ mass)
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < n) generate_star(i, seed, rectangular, corner, corner_abs, mt, pos, mass);
+}
+
+/* Deterministic reduction of the star statistics of include/star.cuh:124-161
+   by one block of 1024 threads (the summation order is fixed by the block
+   size): total mass, sum m^2, sum m^2 ln m, min, max. */
+CCF_D void star_stats_block(int n, const double* __restrict__ mass, double* out)
 {
 	__shared__ double s_m[1024], s_m2[1024], s_l[1024], s_lo[1024], s_hi[1024];
 	double m1 = 0, m2 = 0, ml = 0, lo = 1.7976931348623157e308, hi = 2.2250738585072014e-308;
@@ -82,6 +88,31 @@ __global__ void __launch_bounds__(1024) star_stats_kernel(int n, const double* _
 		out[3] = s_lo[0];
 		out[4] = s_hi[0];
 	}
+}
+
+__global__ void __launch_bounds__(1024) star_stats_kernel(int n, const double* __restrict__ mass, double* out)
+{
+	star_stats_block(n, mass, out);
+}
+
+/* The star field of one field per CTA of 1024 threads, for batches: the
+   generated (or uploaded) stars in generation order, their copy that the
+   tree build reorders, and the statistics -- what generate_stars_kernel, the
+   copy and star_stats_kernel do for one field. */
+__global__ void __launch_bounds__(1024) stars_batch_kernel(const BatchSeg* __restrict__ segs)
+{
+	const BatchSeg& S = segs[blockIdx.x];
+	if (S.gen)
+		for (int i = threadIdx.x; i < S.n; i += blockDim.x)
+			generate_star(i, S.seed, S.rectangular, S.corner, S.corner_abs, S.mt, S.star_gen, S.mass);
+	__syncthreads();
+	for (int i = threadIdx.x; i < S.n; i += blockDim.x) S.pos[i] = S.star_gen[i];
+	star_stats_block(S.n, S.mass, S.stats5);
+}
+
+void launch_stars_batch(cudaStream_t s, const BatchSeg* segs, int nseg)
+{
+	if (nseg > 0) stars_batch_kernel<<<nseg, 1024, 0, s>>>(segs);
 }
 
 /* Initial roots of the rows of solved branch centres (row r is the centre

@@ -17,21 +17,25 @@ star order and identical floating-point sums.
 namespace ccf
 {
 
+/* split flag of node n: its stars and its neighbours' exceed the limit
+   (tree_node.cuh:321-345); returns that neighbourhood count */
+CCF_D int tree_flag_node(const TreeDev& T, int n, int limit, int& flag)
+{
+	int ns = T.star_count[n];
+	const int k = T.nbr_count[n];
+	for (int j = 0; j < k; j++) ns += T.star_count[T.nbr[n * MAX_NBR + j]];
+	flag = ns > limit;
+	T.flag[n] = flag;
+	return ns;
+}
+
 /* per-level split flags, and the level's max neighbourhood count and number
-   of split nodes (tree_node.cuh:321-345) */
+   of split nodes */
 __global__ void tree_flag_kernel(TreeDev T, int start, int count, int limit, int* out)
 {
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	int ns = 0, flag = 0;
-	if (i < count)
-	{
-		int n = start + i;
-		ns = T.star_count[n];
-		int k = T.nbr_count[n];
-		for (int j = 0; j < k; j++) ns += T.star_count[T.nbr[n * MAX_NBR + j]];
-		flag = ns > limit;
-		T.flag[n] = flag;
-	}
+	if (i < count) ns = tree_flag_node(T, start + i, limit, flag);
 	/* warp-aggregated, order-independent integer atomics */
 	unsigned full = 0xffffffffu;
 	int mx = ns, cnt = flag;
@@ -47,46 +51,12 @@ __global__ void tree_flag_kernel(TreeDev T, int start, int count, int limit, int
 	}
 }
 
-/* exclusive scan of n ints by one block (n up to a few million) */
 __global__ void __launch_bounds__(1024) scan_kernel(const int* __restrict__ in, int* __restrict__ out, int n)
 {
-	__shared__ int s_warp[32];
-	__shared__ int s_carry;
-	if (threadIdx.x == 0) s_carry = 0;
-	__syncthreads();
-	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	for (int base = 0; base < n; base += blockDim.x)
-	{
-		int i = base + threadIdx.x;
-		int v = i < n ? in[i] : 0;
-		int x = v;
-		for (int o = 1; o < 32; o <<= 1)
-		{
-			int y = __shfl_up_sync(0xffffffffu, x, o);
-			if (lane >= o) x += y;
-		}
-		if (lane == 31) s_warp[warp] = x;
-		__syncthreads();
-		if (warp == 0)
-		{
-			int w = lane < (int)(blockDim.x >> 5) ? s_warp[lane] : 0;
-			for (int o = 1; o < 32; o <<= 1)
-			{
-				int y = __shfl_up_sync(0xffffffffu, w, o);
-				if (lane >= o) w += y;
-			}
-			s_warp[lane] = w;
-		}
-		__syncthreads();
-		int prefix = s_carry + (warp > 0 ? s_warp[warp - 1] : 0) + x - v;
-		if (i < n) out[i] = prefix;
-		__syncthreads();
-		if (threadIdx.x == blockDim.x - 1) s_carry = prefix + v;
-		__syncthreads();
-	}
+	block_exclusive_scan(in, out, n);
 }
 
-__global__ void tree_root_kernel(TreeDev T, double half, int nstars)
+CCF_D void tree_root_node(const TreeDev& T, double half, int nstars)
 {
 	T.center[0] = make_double2(0, 0);
 	T.half[0] = half;
@@ -100,12 +70,14 @@ __global__ void tree_root_kernel(TreeDev T, double half, int nstars)
 	T.p2l_count[0] = 0;
 }
 
-/* children of split nodes (tree_node.cuh:151-177, 355-381) */
-__global__ void tree_children_kernel(TreeDev T, int start, int count, int child_start)
+__global__ void tree_root_kernel(TreeDev T, double half, int nstars)
 {
-	int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= count) return;
-	int n = start + i;
+	tree_root_node(T, half, nstars);
+}
+
+/* children of split node n (tree_node.cuh:151-177, 355-381) */
+CCF_D void tree_children_node(const TreeDev& T, int n, int child_start)
+{
 	if (!T.flag[n]) return;
 	int base = child_start + 4 * T.rank[n];
 	T.child[n] = base;
@@ -128,15 +100,18 @@ __global__ void tree_children_kernel(TreeDev T, int start, int count, int child_
 	}
 }
 
-/* stable split of each split node's stars into its four quadrants, one warp
-   per node (replaces the atomic two-pass sort of tree_node.cuh:392-501) */
-__global__ void tree_partition_kernel(TreeDev T, int start, int count, double2* __restrict__ pos, double* __restrict__ mass,
+__global__ void tree_children_kernel(TreeDev T, int start, int count, int child_start)
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < count) tree_children_node(T, start + i, child_start);
+}
+
+/* stable split of split node n's stars into its four quadrants by one warp
+   (all 32 lanes call it; replaces the atomic two-pass sort of
+   tree_node.cuh:392-501) */
+CCF_D void tree_partition_node(const TreeDev& T, int n, int lane, double2* __restrict__ pos, double* __restrict__ mass,
 	double2* __restrict__ tpos, double* __restrict__ tmass)
 {
-	int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-	int lane = threadIdx.x & 31;
-	if (w >= count) return;
-	int n = start + w;
 	if (!T.flag[n]) return;
 	int s = T.star_start[n], ns = T.star_count[n];
 	if (ns == 0) return;
@@ -195,13 +170,19 @@ __global__ void tree_partition_kernel(TreeDev T, int start, int count, double2* 
 	}
 }
 
-/* neighbour and interaction lists of the new level (tree_node.cuh:183-267) */
-__global__ void tree_neighbors_kernel(TreeDev T, int start, int count, int* err)
+__global__ void tree_partition_kernel(TreeDev T, int start, int count, double2* __restrict__ pos, double* __restrict__ mass,
+	double2* __restrict__ tpos, double* __restrict__ tmass)
 {
-	int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= count) return;
-	int n = start + i;
-	if (T.level[n] == 0) return;
+	int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	if (w >= count) return;   /* warp-uniform */
+	tree_partition_node(T, start + w, threadIdx.x & 31, pos, mass, tpos, tmass);
+}
+
+/* neighbour and interaction lists of node n of a new level
+   (tree_node.cuh:183-267); returns true when a list overflowed */
+CCF_D bool tree_neighbors_node(const TreeDev& T, int n)
+{
+	if (T.level[n] == 0) return false;
 	int p = T.parent[n];
 	double h = T.half[n];
 	double2 c = T.center[n];
@@ -258,7 +239,13 @@ __global__ void tree_neighbors_kernel(TreeDev T, int start, int count, int* err)
 	T.nbr_count[n] = nn;
 	T.m2l_count[n] = nm;
 	T.p2l_count[n] = np;
-	if (overflow) atomicOr(err, 1);
+	return overflow;
+}
+
+__global__ void tree_neighbors_kernel(TreeDev T, int start, int count, int* err)
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < count && tree_neighbors_node(T, start + i)) atomicOr(err, 1);
 }
 
 /* leaf flags for the leaf numbering scan */
@@ -266,6 +253,95 @@ __global__ void leaf_flag_kernel(TreeDev T, int num_nodes, int* flag)
 {
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i < num_nodes) flag[i] = T.child[i] < 0;
+}
+
+/* The whole tree of one field per CTA, for batches of small fields: the
+   node functions of the per-level launches, level after level, with block
+   barriers in place of the host round trips; the same tree, bit for bit.
+   The level list and the error bits go to seg.info for the host. */
+__global__ void __launch_bounds__(1024) tree_batch_kernel(const BatchSeg* __restrict__ segs)
+{
+	__shared__ int s_mx, s_cnt, s_err, s_start, s_count, s_levels;
+	const BatchSeg& S = segs[blockIdx.x];
+	const TreeDev T = S.T;
+	const unsigned full = 0xffffffffu;
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+	int* const lstart = S.info + 3;
+	int* const lcount = S.info + 3 + TREE_MAX_LEVELS + 1;
+	if (tid == 0)
+	{
+		tree_root_node(T, S.root_half, S.n);
+		s_err = 0;
+		s_start = 0;
+		s_count = 1;
+		s_levels = 0;
+		lstart[0] = 0;
+		lcount[0] = 1;
+	}
+	__syncthreads();
+	for (int L = 0;; L++)
+	{
+		const int start = s_start, count = s_count;
+		if (tid == 0)
+		{
+			s_mx = 0;
+			s_cnt = 0;
+		}
+		__syncthreads();
+		int mx = 0, cnt = 0;
+		for (int i = tid; i < count; i += blockDim.x)
+		{
+			int fl;
+			mx = max(mx, tree_flag_node(T, start + i, S.limit, fl));
+			cnt += fl;
+		}
+		mx = (int)__reduce_max_sync(full, (unsigned)mx);
+		cnt = __reduce_add_sync(full, cnt);
+		if (lane == 0)
+		{
+			atomicMax(&s_mx, mx);
+			atomicAdd(&s_cnt, cnt);
+		}
+		__syncthreads();
+		const int nflag = s_cnt;
+		if (s_mx <= S.limit) break;
+		const int child_start = start + count;
+		if (child_start + 4 * nflag > S.node_cap || L + 1 > TREE_MAX_LEVELS)
+		{
+			if (tid == 0) s_err |= 2;
+			break;
+		}
+		block_exclusive_scan(T.flag + start, T.rank + start, count);
+		for (int i = tid; i < count; i += blockDim.x) tree_children_node(T, start + i, child_start);
+		__syncthreads();
+		for (int w = warp; w < count; w += nw) tree_partition_node(T, start + w, lane, S.pos, S.mass, S.tpos, S.tmass);
+		__syncthreads();
+		bool ov = false;
+		for (int i = tid; i < 4 * nflag; i += blockDim.x) ov |= tree_neighbors_node(T, child_start + i);
+		if (ov) atomicOr(&s_err, 1);
+		__syncthreads();
+		if (tid == 0)
+		{
+			s_start = child_start;
+			s_count = 4 * nflag;
+			s_levels = L + 1;
+			lstart[L + 1] = child_start;
+			lcount[L + 1] = 4 * nflag;
+		}
+		__syncthreads();
+	}
+	__syncthreads();
+	if (tid == 0)
+	{
+		S.info[0] = s_levels;
+		S.info[1] = s_start + s_count;
+		S.info[2] = s_err;
+	}
+}
+
+void launch_tree_batch(cudaStream_t s, const BatchSeg* segs, int nseg)
+{
+	if (nseg > 0) tree_batch_kernel<<<nseg, 1024, 0, s>>>(segs);
 }
 
 void launch_tree_root(cudaStream_t s, const TreeDev& T, double half, int nstars)
