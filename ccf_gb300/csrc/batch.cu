@@ -7,9 +7,11 @@ children, partition and neighbour passes, every level's FMM pass, the leaf
 records -- ~50 launches and a dozen host round trips per field.  For a batch
 of small fields the same work runs here with one CTA per field and a
 handful of launches for the whole batch (stars_batch_kernel,
-tree_batch_kernel, fmm_batch_kernel, leaf_batch_kernel), each a loop over
-the per-field work with block barriers where the per-field path has launch
-boundaries.  The kernels call the same node functions as the per-level
+tree_batch_kernel, leaf_batch_kernel), each a loop over the per-field work
+with block barriers where the per-field path has launch boundaries; the FMM
+passes run level by level over every field at once (fmm_level_batch_kernel:
+one warp per node, the fields side by side), as one CTA per field leaves
+the FP64 translations of a level without the GPU's parallelism.  The kernels call the same node functions as the per-level
 launches, so every field's tree, expansions and leaf records are bit for bit
 those of the per-field path (tests/test_batch_gpu.py compares a batch with
 its fields run one by one).  Host round trips: one after each launch, for
@@ -25,6 +27,48 @@ a tree deeper than its node capacity) runs the per-field path.
 
 namespace ccf
 {
+
+/* the small arrays of a batch's fields from one packed copy: block i copies
+   item i (8-byte words; every item is a whole number of them) */
+struct UploadItem
+{
+	unsigned long long dst, off, bytes;
+};
+__global__ void scatter_uploads_kernel(const char* __restrict__ base, const UploadItem* __restrict__ items)
+{
+	const UploadItem it = items[blockIdx.x];
+	const unsigned long long* src = reinterpret_cast<const unsigned long long*>(base + it.off);
+	unsigned long long* dst = reinterpret_cast<unsigned long long*>(it.dst);
+	for (unsigned long long i = threadIdx.x; i < it.bytes / 8; i += blockDim.x) dst[i] = src[i];
+}
+
+ccf_status Engine::flush_uploads(UploadPack& up)
+{
+	if (up.items.empty()) return CCF_OK;
+	const size_t head = (up.bytes.size() + 15) & ~(size_t)15;
+	const size_t total = head + up.items.size() * sizeof(UploadItem);
+	CCF_TRY(upload_host.ensure(total), "cudaHostAlloc(uploads)");
+	CCF_TRY(upload_dev.ensure(total), "cudaMalloc(uploads)");
+	char* h = static_cast<char*>(upload_host.ptr);
+	std::memcpy(h, up.bytes.data(), up.bytes.size());
+	UploadItem* items = reinterpret_cast<UploadItem*>(h + head);
+	for (size_t i = 0; i < up.items.size(); i++)
+	{
+		if (up.items[i].bytes % 8 != 0 || reinterpret_cast<uintptr_t>(up.items[i].dst) % 8 != 0)
+		{
+			error = "Error. Internal: an upload is not a whole number of 8-byte words.";
+			return CCF_ERR_INVALID_ARGUMENT;
+		}
+		items[i] = {reinterpret_cast<unsigned long long>(up.items[i].dst), up.items[i].off, up.items[i].bytes};
+	}
+	CCF_TRY(cudaMemcpyAsync(upload_dev.ptr, h, total, cudaMemcpyHostToDevice, stream), "uploads");
+	scatter_uploads_kernel<<<(unsigned)up.items.size(), 128, 0, stream>>>(upload_dev.ptr,
+		reinterpret_cast<const UploadItem*>(upload_dev.ptr + head));
+	CCF_TRY(cudaGetLastError(), "scatter_uploads_kernel");
+	up.bytes.clear();
+	up.items.clear();
+	return CCF_OK;
+}
 
 /* stars per field up to which a field's setup runs in one CTA */
 constexpr int BATCH_SETUP_MAX_STARS = 8192;
@@ -136,8 +180,10 @@ ccf_status Engine::prepare_batch(std::vector<Field*>& fields, int verbose)
 		f.info.leaf_max_stars = seg[i].limit;
 	}
 
-	/* FMM passes and leaf numbering */
+	/* FMM passes and leaf numbering; the binomial tables (the entries do not
+	   depend on the table's size) once per kind for the largest order */
 	std::vector<int> order(nf, 0);
+	int maxP[2] = {0, 0};
 	for (int i = 0; i < nf; i++)
 	{
 		if (alone[i]) continue;
@@ -145,10 +191,22 @@ ccf_status Engine::prepare_batch(std::vector<Field*>& fields, int verbose)
 		const int levels = (int)f.level_start.size() - 1;
 		ccf_status rc = fmm_order(f, levels, order[i]);
 		if (rc != CCF_OK) return fail(f, rc);
+		int& m = maxP[f.params.exact_binomials ? 0 : 1];
+		m = std::max(m, order[i]);
+	}
+	for (int k = 0; k < 2; k++)
+		if (maxP[k] > 0)
+		{
+			std::vector<double> B = binomial_table(2 * maxP[k], k == 1);
+			CCF_TRY(batch_binom[k].ensure(B.size()), "cudaMalloc(binomials)");
+			CCF_TRY(cudaMemcpyAsync(batch_binom[k].ptr, B.data(), B.size() * sizeof(double), cudaMemcpyHostToDevice, s),
+				"binomials");
+		}
+	for (int i = 0; i < nf; i++)
+	{
+		if (alone[i]) continue;
+		Field& f = *fields[i];
 		const int P = order[i];
-		std::vector<double> B = binomial_table(2 * P, !f.params.exact_binomials);
-		CCF_TRY(f.binom.ensure(B.size()), "cudaMalloc(binomials)");
-		CCF_TRY(cudaMemcpyAsync(f.binom.ptr, B.data(), B.size() * sizeof(double), cudaMemcpyHostToDevice, s), "binomials");
 		const size_t nc = (size_t)f.num_nodes * (P + 1);
 		CCF_TRY(f.multi.ensure(nc), "cudaMalloc(multipole)");
 		CCF_TRY(f.local.ensure(nc), "cudaMalloc(local)");
@@ -158,7 +216,7 @@ ccf_status Engine::prepare_batch(std::vector<Field*>& fields, int verbose)
 		BatchSeg& g = seg[i];
 		g.T = f.tree_dev();
 		g.P = P;
-		g.B = f.binom.ptr;
+		g.B = batch_binom[f.params.exact_binomials ? 0 : 1].ptr;
 		g.multi = f.multi.ptr;
 		g.local = f.local.ptr;
 		g.leaf_flag = f.leaf_flag.ptr;
@@ -179,10 +237,24 @@ ccf_status Engine::prepare_batch(std::vector<Field*>& fields, int verbose)
 			if (slot[i] >= 0) packed[slot[i]] = seg[i];
 		return cudaMemcpyAsync(batch_segs.ptr, packed.data(), nb * sizeof(BatchSeg), cudaMemcpyHostToDevice, s);
 	};
+	/* this batch's launches: stars, tree, the FMM's zeroing, levels and leaf
+	   numbering, leaf records, the uploads' scatter */
+	int launches = 2;
 	if (nb > 0)
 	{
+		int max_levels = 0, max_level_nodes = 0;
+		long long max_coef = 0;
+		for (int i = 0; i < nf; i++)
+		{
+			if (alone[i]) continue;
+			const Field& f = *fields[i];
+			max_levels = std::max(max_levels, (int)f.level_start.size() - 1);
+			for (int c : f.level_count) max_level_nodes = std::max(max_level_nodes, c);
+			max_coef = std::max(max_coef, (long long)f.num_nodes * (order[i] + 1));
+		}
 		CCF_TRY(upload_packed(), "upload(batch)");
-		launch_fmm_batch(s, batch_segs.ptr, nb);
+		launch_fmm_batch(s, batch_segs.ptr, nb, max_levels, max_level_nodes, max_coef);
+		launches += 2 + (max_levels + 1) + std::max(0, max_levels - 1) + 1 + 1;
 		CCF_TRY(cudaGetLastError(), "fmm_batch_kernel");
 		CCF_TRY(read_info(), "fmm_batch_kernel");
 	}
@@ -238,6 +310,7 @@ ccf_status Engine::prepare_batch(std::vector<Field*>& fields, int verbose)
 
 	/* smooth-mass polynomials, folds, device views, outputs; the fields that
 	   run alone take the per-field path from their tree on */
+	UploadPack up;
 	for (int i = 0; i < nf; i++)
 	{
 		Field& f = *fields[i];
@@ -250,16 +323,18 @@ ccf_status Engine::prepare_batch(std::vector<Field*>& fields, int verbose)
 		else
 		{
 			const int* fi = info.data() + (size_t)i * BATCH_INFO_INTS;
-			rc = finish_view(f, order[i], (double)fi[LEAF_INFO + 1], fi[LEAF_INFO + 2]);
+			rc = finish_view(f, order[i], (double)fi[LEAF_INFO + 1], fi[LEAF_INFO + 2], &up);
 		}
 		if (rc != CCF_OK) return fail(f, rc);
 		CCF_TRY(cudaEventRecord(f.ev[2], s), "event");
 		rc = setup_outputs(f);
 		if (rc != CCF_OK) return fail(f, rc);
-		/* the batch's four launches are counted once, with its first field;
-		   a field's fold is its own launch */
-		if (!alone[i]) f.info.kernel_launches = (i == 0 ? 4 : 0) + (f.info.leaves_folded > 0 ? 1 : 0);
+		/* the batch's launches are counted once, with its first field; a
+		   field's fold is its own launch */
+		if (!alone[i]) f.info.kernel_launches = (i == 0 ? launches : 0) + (f.info.leaves_folded > 0 ? 1 : 0);
 	}
+	ccf_status rc = flush_uploads(up);
+	if (rc != CCF_OK) return rc;
 	if (verbose >= 1) std::cout << "Done setting up " << nf << " fields.\n";
 	return CCF_OK;
 }

@@ -559,9 +559,19 @@ ccf_status Engine::build_fmm(Field& f)
 /* the smooth-mass polynomials, the fold of their series into the leaf
    expansions (rectangular Taylor form, mixed precision) and the field's
    device view, after the leaf records */
-ccf_status Engine::finish_view(Field& f, int P, double near_sum, int lerr)
+ccf_status Engine::finish_view(Field& f, int P, double near_sum, int lerr, UploadPack* up)
 {
 	cudaStream_t s = stream;
+	/* host-to-device copies of small arrays: collected in up when given
+	   (written by one copy and one scatter launch for a whole batch) */
+	auto put = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+		if (up)
+		{
+			up->add(dst, src, bytes);
+			return cudaSuccess;
+		}
+		return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
+	};
 	ccf_params& p = f.params;
 	Derived& d = f.d;
 	const int nl = f.num_leaves;
@@ -605,16 +615,16 @@ ccf_status Engine::finish_view(Field& f, int P, double near_sum, int lerr)
 		inv_corner_df = split4(sp.inv_corner);
 		CCF_TRY(f.sm_d1_df.ensure(d1df.size()), "cudaMalloc(smooth)");
 		CCF_TRY(f.sm_a_df.ensure(adf.size()), "cudaMalloc(smooth)");
-		CCF_TRY(cudaMemcpyAsync(f.sm_d1_df.ptr, d1df.data(), d1df.size() * sizeof(float4), cudaMemcpyHostToDevice, s), "smooth");
-		CCF_TRY(cudaMemcpyAsync(f.sm_a_df.ptr, adf.data(), adf.size() * sizeof(float4), cudaMemcpyHostToDevice, s), "smooth");
+		CCF_TRY(put(f.sm_d1_df.ptr, d1df.data(), d1df.size() * sizeof(float4)), "smooth");
+		CCF_TRY(put(f.sm_a_df.ptr, adf.data(), adf.size() * sizeof(float4)), "smooth");
 		CCF_TRY(f.sm_d1.ensure(d1.size()), "cudaMalloc(smooth)");
 		CCF_TRY(f.sm_d2.ensure(d2.size()), "cudaMalloc(smooth)");
 		CCF_TRY(f.sm_d2f.ensure(d2f.size()), "cudaMalloc(smooth)");
 		CCF_TRY(f.sm_a.ensure(a.size()), "cudaMalloc(smooth)");
-		CCF_TRY(cudaMemcpyAsync(f.sm_d1.ptr, d1.data(), d1.size() * sizeof(double2), cudaMemcpyHostToDevice, s), "smooth");
-		CCF_TRY(cudaMemcpyAsync(f.sm_d2.ptr, d2.data(), d2.size() * sizeof(double2), cudaMemcpyHostToDevice, s), "smooth");
-		CCF_TRY(cudaMemcpyAsync(f.sm_d2f.ptr, d2f.data(), d2f.size() * sizeof(float2), cudaMemcpyHostToDevice, s), "smooth");
-		CCF_TRY(cudaMemcpyAsync(f.sm_a.ptr, a.data(), a.size() * sizeof(double2), cudaMemcpyHostToDevice, s), "smooth");
+		CCF_TRY(put(f.sm_d1.ptr, d1.data(), d1.size() * sizeof(double2)), "smooth");
+		CCF_TRY(put(f.sm_d2.ptr, d2.data(), d2.size() * sizeof(double2)), "smooth");
+		CCF_TRY(put(f.sm_d2f.ptr, d2f.data(), d2f.size() * sizeof(float2)), "smooth");
+		CCF_TRY(put(f.sm_a.ptr, a.data(), a.size() * sizeof(double2)), "smooth");
 		/* the tracker's leaf blocks with the Taylor series folded in (rectangular
 		   Taylor smooth mass, mixed precision): the series conjugated into
 		   polynomials in z, built in long double */
@@ -712,7 +722,7 @@ ccf_status Engine::finish_view(Field& f, int P, double near_sum, int lerr)
 	V.leaf_loc3f_fold = fold_ok ? f.leaf_loc3f_fold.ptr : nullptr;
 	V.leaf_loc_fold64 = fold_ok ? f.leaf_loc_fold64.ptr : nullptr;
 	CCF_TRY(f.view_dev.ensure(1), "cudaMalloc(view)");
-	CCF_TRY(cudaMemcpyAsync(f.view_dev.ptr, &V, sizeof(V), cudaMemcpyHostToDevice, s), "view");
+	CCF_TRY(put(f.view_dev.ptr, &V, sizeof(V)), "view");
 	return CCF_OK;
 }
 
@@ -810,6 +820,10 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 	std::vector<double> cost_i, cost_c;
 	long long table_slots = 0;   /* tracker: 2 R slots per phi step of every continuation row */
 	std::vector<int> item_start_host(2 * nb_total(fields));
+	std::vector<SeedSeg> seeds;
+	long long max_seeds = 0;
+	/* fields with the same branches and phi steps share one phase table */
+	std::vector<std::pair<std::pair<int, int>, const PhaseEntry*>> phase_tables;
 	for (int i = 0; i < nf; i++)
 	{
 		Field& f = *fields[i];
@@ -834,9 +848,18 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		o.seg = seg[i];
 		if (track)
 		{
-			CCF_TRY(f.phase.ensure(f.params.num_phi), "cudaMalloc(phase)");
-			CCF_TRY(launch_phase_table(s, nb, f.params.num_phi, f.phase.ptr), "phase_table_kernel");
-			o.phase = f.phase.ptr;
+			const std::pair<int, int> key(nb, f.params.num_phi);
+			const PhaseEntry* shared = nullptr;
+			for (const auto& t : phase_tables)
+				if (t.first == key) shared = t.second;
+			if (!shared)
+			{
+				CCF_TRY(f.phase.ensure(f.params.num_phi), "cudaMalloc(phase)");
+				CCF_TRY(launch_phase_table(s, nb, f.params.num_phi, f.phase.ptr), "phase_table_kernel");
+				shared = f.phase.ptr;
+				phase_tables.push_back({key, shared});
+			}
+			o.phase = shared;
 		}
 		o.cont_master = P.master_cont.ptr;
 		o.cont_snap32 = mixed ? P.snap32_cont.ptr : nullptr;
@@ -875,10 +898,29 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		   next to neighbouring stars, in the same or adjacent leaves, so their
 		   near-star loops and smooth-mass paths agree (the order of the roots
 		   within a column carries no meaning; a row stays one root's path) */
-		launch_seed_roots(s, N, R, K, f.star_pos.ptr, f.star_mass.ptr, f.view.corner_abs, f.view.theta,
-			1 - f.view.kappa_tot + f.view.kappa_star, f.view.shear, nb, g, P.master_init.ptr + init_off[i],
-			mixed ? P.snap32_init.ptr + init_off[i] : nullptr, mixed ? nullptr : P.snap64_init.ptr + init_off[i]);
+		SeedSeg sd;
+		sd.nstars = N;
+		sd.nroots = R;
+		sd.nrows = K;
+		sd.nb = nb;
+		sd.seg = g;
+		sd.pos = f.star_pos.ptr;
+		sd.mass = f.star_mass.ptr;
+		sd.corner_abs = f.view.corner_abs;
+		sd.theta = f.view.theta;
+		sd.a_lin = 1 - f.view.kappa_tot + f.view.kappa_star;
+		sd.gamma = f.view.shear;
+		sd.master = P.master_init.ptr + init_off[i];
+		sd.snap32 = mixed ? P.snap32_init.ptr + init_off[i] : nullptr;
+		sd.snap64 = mixed ? nullptr : P.snap64_init.ptr + init_off[i];
+		seeds.push_back(sd);
+		max_seeds = std::max(max_seeds, (long long)R * K);
 	}
+	/* every field's seeds in one launch */
+	CCF_TRY(P.seeds.ensure(seeds.size()), "cudaMalloc(seeds)");
+	CCF_TRY(cudaMemcpyAsync(P.seeds.ptr, seeds.data(), seeds.size() * sizeof(SeedSeg), cudaMemcpyHostToDevice, s), "upload");
+	launch_seed_roots_batch(s, P.seeds.ptr, (int)seeds.size(), max_seeds);
+	CCF_TRY(cudaGetLastError(), "seed_roots_batch_kernel");
 	/* largest rows first */
 	auto order = [](std::vector<RowDesc>& rows, std::vector<double>& cost) {
 		std::vector<int> idx(rows.size());

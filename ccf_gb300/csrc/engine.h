@@ -8,6 +8,7 @@ CCF<T>::run / save, include/ccf.cuh:1265-1287) and of batches of fields.
 #include "params.h"
 
 #include <cuda_runtime.h>
+#include <cstring>
 
 #include <memory>
 #include <string>
@@ -213,6 +214,28 @@ struct SolverPools
 	DBuf<FieldOut> outs;
 	DBuf<const float4*> hilo_ptrs;
 	DBuf<int> error;
+	DBuf<SeedSeg> seeds;
+};
+
+/* small host-to-device copies collected for one copy of the packed bytes and
+   one scatter launch (batch.cu flush_uploads): the sources are copied into
+   the pack at once, so they need not outlive add() */
+struct UploadPack
+{
+	struct Item
+	{
+		void* dst;
+		size_t off, bytes;
+	};
+	std::vector<char> bytes;
+	std::vector<Item> items;
+	void add(void* dst, const void* src, size_t n)
+	{
+		const size_t off = (bytes.size() + 15) & ~(size_t)15;
+		bytes.resize(off + n);
+		std::memcpy(bytes.data() + off, src, n);
+		items.push_back({dst, off, n});
+	}
 };
 
 /* inside an Engine member returning ccf_status: a CUDA error becomes the
@@ -263,7 +286,8 @@ private:
 	ccf_status fmm_order(Field& f, int levels, int& P);
 	ccf_status setup_begin(Field& f, int verbose);
 	void setup_stats(Field& f, const double* st);
-	ccf_status finish_view(Field& f, int P, double near_sum, int lerr);
+	ccf_status finish_view(Field& f, int P, double near_sum, int lerr, UploadPack* up = nullptr);
+	ccf_status flush_uploads(UploadPack& up);
 	ccf_status setup_outputs(Field& f);
 	ccf_status prepare_batch(std::vector<Field*>& fields, int verbose);
 	ccf_status solve(std::vector<Field*>& fields, int verbose);
@@ -295,6 +319,9 @@ private:
 	DBuf<BatchSeg> batch_segs;
 	DBuf<int> batch_info;
 	DBuf<double> batch_stats;
+	DBuf<double> batch_binom[2];   /* binomial tables: exact, the reference's int32 one */
+	DBuf<char> upload_dev;         /* packed small uploads and their item list */
+	HostBuf upload_host;
 	/* batch setup: engines (their streams) of the setup threads, and events */
 	std::vector<std::unique_ptr<Engine>> setup_workers;
 	std::vector<cudaEvent_t> setup_events;

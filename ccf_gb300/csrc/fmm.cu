@@ -543,41 +543,42 @@ void launch_fold_smooth(cudaStream_t s, int num_leaves, int P, const double2* le
 namespace ccf
 {
 
-/* The FMM passes of one field per CTA, for batches: the upward pass level
-   by level from the leaves, the downward pass from level 2, then the leaf
-   numbering -- the node functions of the per-level launches, with block
-   barriers between levels.  The leaf count goes to seg.info for the host. */
-__global__ void __launch_bounds__(512) fmm_batch_kernel(const BatchSeg* __restrict__ segs)
+/* The FMM passes of a batch, level by level over every field at once:
+   blockIdx.y is the field, the x blocks take four of its nodes of level L
+   each (one warp per node, as fmm_upward_kernel / fmm_downward_kernel do
+   for one field); a field without that level, or with fewer nodes there,
+   leaves its extra blocks idle.  The expansions start from zero (the first
+   kernel), and the leaf numbering takes one CTA per field (the last). */
+__global__ void fmm_zero_batch_kernel(const BatchSeg* __restrict__ segs)
 {
-	const BatchSeg& S = segs[blockIdx.x];
-	const TreeDev T = S.T;
-	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-	const int levels = S.info[0], nodes = S.info[1], P = S.P;
-	const int* lstart = S.info + 3;
-	const int* lcount = S.info + 3 + TREE_MAX_LEVELS + 1;
-	const size_t nc = (size_t)nodes * (P + 1);
-	for (size_t i = tid; i < nc; i += blockDim.x)
+	const BatchSeg& S = segs[blockIdx.y];
+	const size_t nc = (size_t)S.info[1] * (S.P + 1);
+	for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nc; i += (size_t)gridDim.x * blockDim.x)
 	{
 		S.multi[i] = make_double2(0, 0);
 		S.local[i] = make_double2(0, 0);
 	}
-	__syncthreads();
-	for (int L = levels; L >= 0; L--)
-	{
-		const int st = lstart[L], cnt = lcount[L];
-		for (int w = warp; w < cnt; w += nw) fmm_upward_node(T, st + w, P, lane, S.pos, S.mass, S.multi, S.B);
-		__syncthreads();
-	}
-	for (int L = 2; L <= levels; L++)
-	{
-		const int st = lstart[L], cnt = lcount[L];
-		for (int w = warp; w < cnt; w += nw) fmm_downward_node(T, st + w, P, lane, S.pos, S.mass, S.multi, S.local, S.B);
-		__syncthreads();
-	}
-	for (int i = tid; i < nodes; i += blockDim.x) S.leaf_flag[i] = T.child[i] < 0;
+}
+
+__global__ void fmm_level_batch_kernel(const BatchSeg* __restrict__ segs, int L, int upward)
+{
+	const BatchSeg& S = segs[blockIdx.y];
+	if (L > S.info[0]) return;
+	const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+	if (w >= S.info[3 + TREE_MAX_LEVELS + 1 + L]) return;   /* warp-uniform */
+	const int n = S.info[3 + L] + w;
+	if (upward) fmm_upward_node(S.T, n, S.P, threadIdx.x & 31, S.pos, S.mass, S.multi, S.B);
+	else fmm_downward_node(S.T, n, S.P, threadIdx.x & 31, S.pos, S.mass, S.multi, S.local, S.B);
+}
+
+__global__ void __launch_bounds__(1024) leaf_number_batch_kernel(const BatchSeg* __restrict__ segs)
+{
+	const BatchSeg& S = segs[blockIdx.x];
+	const int nodes = S.info[1];
+	for (int i = threadIdx.x; i < nodes; i += blockDim.x) S.leaf_flag[i] = S.T.child[i] < 0;
 	__syncthreads();
 	const int nl = block_exclusive_scan(S.leaf_flag, S.leaf_index, nodes);
-	if (tid == 0) S.info[LEAF_INFO] = nl;
+	if (threadIdx.x == 0) S.info[LEAF_INFO] = nl;
 }
 
 /* The leaf records of one field per CTA, for batches: leaf_build_kernel,
@@ -626,9 +627,16 @@ __global__ void __launch_bounds__(512) leaf_batch_kernel(const BatchSeg* __restr
 	}
 }
 
-void launch_fmm_batch(cudaStream_t s, const BatchSeg* segs, int nseg)
+void launch_fmm_batch(cudaStream_t s, const BatchSeg* segs, int nseg, int max_levels, int max_level_nodes,
+	long long max_coefficients)
 {
-	if (nseg > 0) fmm_batch_kernel<<<nseg, 512, 0, s>>>(segs);
+	if (nseg <= 0) return;
+	const int gz = (int)std::min<long long>((max_coefficients + 255) / 256, 64);
+	fmm_zero_batch_kernel<<<dim3(std::max(gz, 1), nseg), 256, 0, s>>>(segs);
+	const int gx = std::max(1, (max_level_nodes + 3) / 4);
+	for (int L = max_levels; L >= 0; L--) fmm_level_batch_kernel<<<dim3(gx, nseg), 128, 0, s>>>(segs, L, 1);
+	for (int L = 2; L <= max_levels; L++) fmm_level_batch_kernel<<<dim3(gx, nseg), 128, 0, s>>>(segs, L, 0);
+	leaf_number_batch_kernel<<<nseg, 1024, 0, s>>>(segs);
 }
 void launch_leaf_batch(cudaStream_t s, const BatchSeg* segs, int nseg)
 {

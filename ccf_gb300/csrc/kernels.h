@@ -366,6 +366,19 @@ CCF_D int block_exclusive_scan(const int* __restrict__ in, int* __restrict__ out
 
 void launch_stars_batch(cudaStream_t s, const BatchSeg* segs, int nseg);
 
+/* the root seeds of one field's solved centres (stars.cu seed_root) */
+struct SeedSeg
+{
+	int nstars, nroots, nrows, nb, seg;
+	const double2* pos;
+	const double* mass;
+	double corner_abs, theta, a_lin, gamma;
+	double2* master;
+	float4* snap32;
+	double2* snap64;
+};
+void launch_seed_roots_batch(cudaStream_t s, const SeedSeg* segs, int nseg, long long max_seeds);
+
 /* tree.cu */
 void launch_tree_batch(cudaStream_t s, const BatchSeg* segs, int nseg);
 void launch_tree_root(cudaStream_t s, const TreeDev& T, double half, int nstars);
@@ -378,7 +391,8 @@ void launch_tree_neighbors(cudaStream_t s, const TreeDev& T, int start, int coun
 void launch_leaf_flag(cudaStream_t s, const TreeDev& T, int num_nodes, int* flag);
 
 /* fmm.cu */
-void launch_fmm_batch(cudaStream_t s, const BatchSeg* segs, int nseg);
+void launch_fmm_batch(cudaStream_t s, const BatchSeg* segs, int nseg, int max_levels, int max_level_nodes,
+	long long max_coefficients);
 void launch_leaf_batch(cudaStream_t s, const BatchSeg* segs, int nseg);
 void launch_fmm_upward(cudaStream_t s, const TreeDev& T, int start, int count, int P, const double2* pos, const double* mass,
 	double2* multi, const double* B);

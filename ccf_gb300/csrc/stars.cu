@@ -125,45 +125,60 @@ void launch_stars_batch(cudaStream_t s, const BatchSeg* segs, int nseg)
    Aberth iteration to the same set of zeros, these in fewer sweeps.  The
    extra roots of the rectangular Taylor form sit evenly on the circle of
    radius |corner|, as in the reference.  Stars in tree order. */
+CCF_D void seed_root(long long q, int nstars, int nroots, const double2* __restrict__ pos, const double* __restrict__ mass,
+	double corner_abs, double theta, double a_lin, double gamma, int nb, int seg, double2* __restrict__ master,
+	float4* __restrict__ snap32, double2* __restrict__ snap64)
+{
+	const int extra = nroots - 2 * nstars;
+	const int row = (int)(q / nroots);
+	const int a = (int)(q % nroots);
+	double2 z;
+	if (a < 2 * nstars)
+	{
+		const int i = a < nstars ? a : a - nstars;
+		const double phi = PI / nb + (row * seg) * 2 * PI / nb;
+		double sp, cp;
+		sincos(phi, &sp, &cp);
+		/* D = a e^{-i phi} - gamma; w = theta sqrt(m) / sqrt(D) */
+		const double dx = a_lin * cp - gamma, dy = -a_lin * sp;
+		const double rd = hypot(dx, dy);
+		double2 w = make_double2(1, 0);
+		if (rd > 1e-6 && mass[i] > 0)
+		{
+			const double r = theta * sqrt(mass[i] / rd), t = -0.5 * atan2(dy, dx);
+			w = make_double2(r * cos(t), r * sin(t));
+		}
+		const double sg = a < nstars ? 1.0 : -1.0;
+		z = make_double2(pos[i].x + sg * w.x, pos[i].y + sg * w.y);
+	}
+	else
+	{
+		const int k = a - 2 * nstars;
+		const double t = 2 * PI / extra * k;
+		z = make_double2(corner_abs * cos(t), corner_abs * sin(t));
+	}
+	master[q] = z;
+	if (snap32) snap32[q] = split_hilo(z);
+	if (snap64) snap64[q] = z;
+}
+
 __global__ void seed_roots_kernel(int nstars, int nroots, int nrows, const double2* __restrict__ pos,
 	const double* __restrict__ mass, double corner_abs, double theta, double a_lin, double gamma, int nb, int seg,
 	double2* __restrict__ master, float4* __restrict__ snap32, double2* __restrict__ snap64)
 {
-	long long total = (long long)nrows * nroots;
-	int extra = nroots - 2 * nstars;
+	const long long total = (long long)nrows * nroots;
 	for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x)
-	{
-		const int row = (int)(q / nroots);
-		int a = (int)(q % nroots);
-		double2 z;
-		if (a < 2 * nstars)
-		{
-			const int i = a < nstars ? a : a - nstars;
-			const double phi = PI / nb + (row * seg) * 2 * PI / nb;
-			double sp, cp;
-			sincos(phi, &sp, &cp);
-			/* D = a e^{-i phi} - gamma; w = theta sqrt(m) / sqrt(D) */
-			const double dx = a_lin * cp - gamma, dy = -a_lin * sp;
-			const double rd = hypot(dx, dy);
-			double2 w = make_double2(1, 0);
-			if (rd > 1e-6 && mass[i] > 0)
-			{
-				const double r = theta * sqrt(mass[i] / rd), t = -0.5 * atan2(dy, dx);
-				w = make_double2(r * cos(t), r * sin(t));
-			}
-			const double sg = a < nstars ? 1.0 : -1.0;
-			z = make_double2(pos[i].x + sg * w.x, pos[i].y + sg * w.y);
-		}
-		else
-		{
-			int i = a - 2 * nstars;
-			double t = 2 * PI / extra * i;
-			z = make_double2(corner_abs * cos(t), corner_abs * sin(t));
-		}
-		master[q] = z;
-		if (snap32) snap32[q] = split_hilo(z);
-		if (snap64) snap64[q] = z;
-	}
+		seed_root(q, nstars, nroots, pos, mass, corner_abs, theta, a_lin, gamma, nb, seg, master, snap32, snap64);
+}
+
+/* the seeds of every field of a batch in one launch: blockIdx.y is the field */
+__global__ void seed_roots_batch_kernel(const SeedSeg* __restrict__ segs)
+{
+	const SeedSeg& S = segs[blockIdx.y];
+	const long long total = (long long)S.nrows * S.nroots;
+	for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x)
+		seed_root(q, S.nstars, S.nroots, S.pos, S.mass, S.corner_abs, S.theta, S.a_lin, S.gamma, S.nb, S.seg, S.master,
+			S.snap32, S.snap64);
 }
 
 /* FP32 hi/lo form of the star positions (the poles of the Aberth sums) and,
@@ -200,6 +215,13 @@ void launch_seed_roots(cudaStream_t s, int nstars, int nroots, int nrows, const 
 	int blocks = (int)std::min<long long>((total + 255) / 256, 152 * 16);
 	seed_roots_kernel<<<blocks, 256, 0, s>>>(nstars, nroots, nrows, pos, mass, corner_abs, theta, a_lin, gamma, nb, seg,
 		master, snap32, snap64);
+}
+
+void launch_seed_roots_batch(cudaStream_t s, const SeedSeg* segs, int nseg, long long max_seeds)
+{
+	if (nseg <= 0) return;
+	const int gx = (int)std::min<long long>((max_seeds + 255) / 256, 152 * 4);
+	seed_roots_batch_kernel<<<dim3(gx, nseg), 256, 0, s>>>(segs);
 }
 
 void launch_star_hilo(cudaStream_t s, int n, const double2* pos, float4* out, const double* mass, float2* mass_out)

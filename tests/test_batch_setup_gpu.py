@@ -66,7 +66,7 @@ def test_batched_setup_is_the_per_field_setup(precision):
 
 
 def test_batched_setup_launches():
-    """a batch of small fields: the setup's four launches for the whole batch,
+    """a batch of small fields: the setup's launches for the whole batch,
     counted with its first field"""
     fields = [make(disc_field(n, 900 + n), "mixed") for n in (60, 200, 450, 700, 950)]
     assert run_batch(fields, -1), fields[0].last_error()
