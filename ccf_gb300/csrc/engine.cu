@@ -995,6 +995,7 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 	A.fin = P.fin_cont.ptr;
 	A.list = P.list_cont.ptr;
 	A.fval = P.fval_cont.ptr;
+	bool reorder = false;
 	if (track)
 	{
 		/* every root on its own path; rows that fail the column check run
@@ -1032,7 +1033,14 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		CCF_TRY(cudaMemsetAsync(P.row_stats.ptr, 0, TRACK_ROW_STATS * rc.size() * sizeof(unsigned long long), s), "memset");
 		CCF_TRY(cudaMemsetAsync(P.rerun_count.ptr, 0, 6 * sizeof(int), s), "memset");
 		CCF_TRY(cudaMemsetAsync(P.row_stats2.ptr, 0, TRACK_ROW_STATS * rc.size() * sizeof(unsigned long long), s), "memset");
+		CCF_TRY(P.item_order.ensure((size_t)T.num_items + 1), "cudaMalloc(items)");
+		CCF_TRY(P.item_work.ensure(2 * (size_t)T.num_items + 2), "cudaMalloc(items)");
+		/* long items first where the launch is a few waves of items, and its
+		   last wave's length is a sizeable share of it (track_item_order_kernel) */
+		reorder = (long long)T.num_items < 32LL * num_sms * TRACK_WARPS_PER_SM;
+		T.item_order = reorder ? P.item_order.ptr : nullptr;
 		CCF_TRY(launch_track_mark(s, T), "track_mark");
+		if (reorder) CCF_TRY(launch_track_item_order(s, T, P.item_work.ptr, P.item_order.ptr), "track_item_order");
 		CCF_TRY(launch_track(s, T, mixed), "track_ccs");
 		CCF_TRY(launch_track_check(s, T, max_row_points), "track_check");
 		CCF_TRY(launch_collect_rerun(s, T, P.rows_rerun.ptr, P.rerun_count.ptr), "collect_rerun");
@@ -1041,6 +1049,7 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		   the fifth power of the step), then the rows failing still go to the
 		   full-sum solver; all on device-side row counts */
 		TrackArgs T2 = T;
+		T2.item_order = nullptr;
 		T2.rows = P.rows_rerun.ptr;
 		T2.num_rows_dev = P.rerun_count.ptr;
 		T2.items_per_row = (maxR + 31) / 32;
@@ -1088,13 +1097,13 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 
 	ccf_status status = CCF_OK;
 	/* root seeds, initial solve, continuation (tracker: phase table, item
-	   marking, tracking, column check, row collection, table clearing,
+	   marking, item order (2), tracking, column check, row collection, table clearing,
 	   re-tracking, column check, row collection and the full-sum launch for
 	   the rows to re-run), FP64 polish; the launches are shared by the
 	   batch's fields and counted with the first */
 	for (int fi = 0; fi < nf; fi++)
 	{
-		ccf_status rc = finish_stats(*fields[fi], seg[fi], track, verbose, fi > 0 ? 0 : track ? 14 : 5);
+		ccf_status rc = finish_stats(*fields[fi], seg[fi], track, verbose, fi > 0 ? 0 : track ? (reorder ? 16 : 14) : 5);
 		if (rc != CCF_OK) status = rc;
 	}
 	return status;

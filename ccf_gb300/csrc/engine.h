@@ -215,6 +215,7 @@ struct SolverPools
 	DBuf<const float4*> hilo_ptrs;
 	DBuf<int> error;
 	DBuf<SeedSeg> seeds;
+	DBuf<int> item_order, item_work;   /* tracker: the queue order of the items, and its scratch */
 };
 
 /* small host-to-device copies collected for one copy of the packed bytes and

@@ -245,6 +245,7 @@ struct TrackArgs
 	int2* solo;                 /* (row, root) of the roots that start off the root box: one warp each, first ... */
 	int* num_solo;              /* ... their number (zeroed before the marking launch) */
 	unsigned char* is_solo;     /* [master index]: the root runs solo, not in its item */
+	const int* item_order;      /* [num_items]: the queue's order of the items; null: in order */
 	/* re-tracking of rows that failed the check: the rows are a device-side
 	   list of *num_rows_dev rows, items_per_row fixed-size items each (no
 	   solo roots), and a phi sub-step never longer than max_sub */
@@ -413,6 +414,8 @@ void launch_fold_smooth(cudaStream_t s, int num_leaves, int P, const double2* le
 int solver_blocks_per_sm(bool mixed);
 cudaError_t launch_solve(cudaStream_t s, const SolveArgs& a, bool mixed, bool initial);
 cudaError_t launch_track_mark(cudaStream_t s, const TrackArgs& a);
+cudaError_t launch_track_item_order(cudaStream_t s, const TrackArgs& a, int* work, int* order);
+constexpr int TRACK_WARPS_PER_SM = 12;   /* resident tracker warps per SM (3 CTAs of 4 warps) */
 cudaError_t launch_phase_table(cudaStream_t s, int nb, int nphi, PhaseEntry* out);
 cudaError_t launch_track(cudaStream_t s, const TrackArgs& a, bool mixed);
 cudaError_t launch_track_check(cudaStream_t s, const TrackArgs& a, long long max_row_points);

@@ -1206,6 +1206,8 @@ __global__ void __launch_bounds__(TNT, 3) track_kernel(const TrackArgs T)
 		else if (solo_root < 0)
 		{
 			if (item >= T.num_items) break;
+			/* the queue's order of the items (track_item_order_kernel) */
+			if (T.item_order) item = T.item_order[item];
 			row = item_row(T, item);
 		}
 		row = __shfl_sync(full, row, 0);
@@ -1572,6 +1574,60 @@ __global__ void collect_rerun_kernel(const TrackArgs T, RowDesc* rerun, int* cou
 		atomicMax(&st[6], rs[2]);
 		if (rs[3]) atomicAdd(&st[4], rs[3]);
 	}
+}
+
+/* The queue order of the tracker's work items: the items holding a root
+   whose |f'| at the branch centre is below TRACK_SLOW_DF / theta_star first.
+   Such roots move fast along the curve (dz/dphi = i a e^{-i phi} / f'),
+   where the predictor misses the 1e-9 theta_star tolerance and the
+   corrector takes a second evaluation at most steps; their items run ~1.4
+   times longer.  A launch of persistent warps ends one item after its queue
+   empties (on the bench field the SMs idled 20 % of the launch), so the long
+   items go first and the launch ends on short ones.  The items keep their
+   roots; only the order changes, and with it nothing in the results.
+   flag: one warp per item, a lane per root (solo roots do not run in their
+   item); order: one CTA, a stable partition by block scans. */
+constexpr float TRACK_SLOW_DF = 1.0f;
+
+__global__ void track_item_flag_kernel(const TrackArgs T, int* flag)
+{
+	const int item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	const int lane = threadIdx.x & 31;
+	if (item >= T.num_items) return;   /* warp-uniform */
+	const int row = item_row(T, item);
+	const RowDesc rd = T.rows[row];
+	const FieldView& F = T.fields[rd.field];
+	const int a = (item - T.item_start[row]) * 32 + lane;
+	bool slow = false;
+	if (a < F.num_roots && !T.is_solo[rd.base + a])
+	{
+		const double2 z = T.master[rd.base + a];
+		const int leaf = find_leaf(F, z);
+		if (leaf >= 0)
+		{
+			const float2 d = eval_df32(F, leaf, z, make_double2(0, 0));
+			slow = hypotf(d.x, d.y) * (float)F.theta < TRACK_SLOW_DF;
+		}
+	}
+	const bool any = __any_sync(0xffffffffu, slow);
+	if (lane == 0) flag[item] = any ? 0 : 1;   /* 0: first */
+}
+
+__global__ void __launch_bounds__(1024) track_item_order_kernel(int n, int* flag, int* rank, int* order)
+{
+	/* rank = exclusive scan of flag (the fast items before each item) */
+	const int fast = block_exclusive_scan(flag, rank, n);
+	const int nslow = n - fast;
+	for (int i = threadIdx.x; i < n; i += blockDim.x)
+		order[flag[i] ? nslow + rank[i] : i - rank[i]] = i;
+}
+
+cudaError_t launch_track_item_order(cudaStream_t s, const TrackArgs& a, int* work, int* order)
+{
+	if (a.num_items == 0) return cudaSuccess;
+	track_item_flag_kernel<<<(a.num_items + 3) / 4, 128, 0, s>>>(a, work);
+	track_item_order_kernel<<<1, 1024, 0, s>>>(a.num_items, work, work + a.num_items, order);
+	return cudaGetLastError();
 }
 
 cudaError_t launch_track_mark(cudaStream_t s, const TrackArgs& a)

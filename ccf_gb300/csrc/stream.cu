@@ -403,6 +403,7 @@ ccf_status Engine::solve_chunked(Field& f, int verbose)
 	A.fin = P.fin_cont.ptr;
 	A.list = P.list_cont.ptr;
 	A.fval = P.fval_cont.ptr;
+	int reordered_groups = 0;
 	for (int g = 0; g < ngroups; g++)
 	{
 		const int k = g & 1;
@@ -437,11 +438,20 @@ ccf_status Engine::solve_chunked(Field& f, int verbose)
 			CCF_TRY_S(cudaMemsetAsync(P.row_stats.ptr, 0, TRACK_ROW_STATS * grows * sizeof(unsigned long long), s), "memset");
 			CCF_TRY_S(cudaMemsetAsync(P.rerun_count.ptr, 0, 6 * sizeof(int), s), "memset");
 			CCF_TRY_S(cudaMemsetAsync(P.row_stats2.ptr, 0, TRACK_ROW_STATS * grows * sizeof(unsigned long long), s), "memset");
+			CCF_TRY_S(P.item_order.ensure((size_t)T.num_items + 1), "cudaMalloc(items)");
+			CCF_TRY_S(P.item_work.ensure(2 * (size_t)T.num_items + 2), "cudaMalloc(items)");
+			/* long items first where the launch is a few waves of items, and its
+			   last wave's length is a sizeable share of it (track_item_order_kernel) */
+			const bool reorder = (long long)T.num_items < 32LL * num_sms * TRACK_WARPS_PER_SM;
+			if (reorder) reordered_groups++;
+			T.item_order = reorder ? P.item_order.ptr : nullptr;
 			CCF_TRY_S(launch_track_mark(s, T), "track_mark");
+			if (reorder) CCF_TRY_S(launch_track_item_order(s, T, P.item_work.ptr, P.item_order.ptr), "track_item_order");
 			CCF_TRY_S(launch_track(s, T, mixed), "track_ccs");
 			CCF_TRY_S(launch_track_check(s, T, (long long)R * seg * half), "track_check");
 			CCF_TRY_S(launch_collect_rerun(s, T, P.rows_rerun.ptr, P.rerun_count.ptr), "collect_rerun");
 			TrackArgs T2 = T;
+			T2.item_order = nullptr;
 			T2.rows = P.rows_rerun.ptr;
 			T2.num_rows_dev = P.rerun_count.ptr;
 			T2.items_per_row = (R + 31) / 32;
@@ -491,8 +501,9 @@ ccf_status Engine::solve_chunked(Field& f, int verbose)
 	/* seeds, (phase table), initial solve, its polish (2); per group the
 	   tracker's 8 launches (marking, tracking, column check, collection,
 	   table clearing, re-tracking, column check, collection) and the full-sum
-	   launch, or the full-sum launch alone, then the polish (2) */
-	return finish_stats(f, seg, track, verbose, (track ? 5 : 4) + (track ? 11 : 3) * ngroups);
+	   launch, or the full-sum launch alone, then the polish (2); and the item
+	   order's 2 where a group reorders its items */
+	return finish_stats(f, seg, track, verbose, (track ? 5 : 4) + (track ? 11 : 3) * ngroups + 2 * reordered_groups);
 }
 
 } /* namespace ccf */
