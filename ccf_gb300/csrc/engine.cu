@@ -1034,7 +1034,7 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 		CCF_TRY(cudaMemsetAsync(P.rerun_count.ptr, 0, 6 * sizeof(int), s), "memset");
 		CCF_TRY(cudaMemsetAsync(P.row_stats2.ptr, 0, TRACK_ROW_STATS * rc.size() * sizeof(unsigned long long), s), "memset");
 		CCF_TRY(P.item_order.ensure((size_t)T.num_items + 1), "cudaMalloc(items)");
-		CCF_TRY(P.item_work.ensure(2 * (size_t)T.num_items + 2), "cudaMalloc(items)");
+		CCF_TRY(P.item_work.ensure(3 * (size_t)T.num_items + 3), "cudaMalloc(items)");
 		/* long items first where the launch is a few waves of items, and its
 		   last wave's length is a sizeable share of it (track_item_order_kernel) */
 		reorder = (long long)T.num_items < 32LL * num_sms * TRACK_WARPS_PER_SM;

@@ -1576,20 +1576,21 @@ __global__ void collect_rerun_kernel(const TrackArgs T, RowDesc* rerun, int* cou
 	}
 }
 
-/* The queue order of the tracker's work items: the items holding a root
-   whose |f'| at the branch centre is below TRACK_SLOW_DF / theta_star first.
-   Such roots move fast along the curve (dz/dphi = i a e^{-i phi} / f'),
-   where the predictor misses the 1e-9 theta_star tolerance and the
-   corrector takes a second evaluation at most steps; their items run ~1.4
-   times longer.  A launch of persistent warps ends one item after its queue
+/* The queue order of the tracker's work items: by the smallest |f'| of
+   their roots at the branch centre, smallest first, in TRACK_ORDER_CLASSES
+   classes of |f'| theta_star (below 0.03, 0.1, 0.3, 1, 3, and the rest).
+   Roots with a small |f'| move fast along the curve (dz/dphi = i a e^{-i phi}
+   / f'), where the predictor misses the 1e-9 theta_star tolerance and the
+   corrector takes a second evaluation at most steps; their items run
+   longer.  A launch of persistent warps ends one item after its queue
    empties (on the bench field the SMs idled 20 % of the launch), so the long
    items go first and the launch ends on short ones.  The items keep their
    roots; only the order changes, and with it nothing in the results.
-   flag: one warp per item, a lane per root (solo roots do not run in their
-   item); order: one CTA, a stable partition by block scans. */
-constexpr float TRACK_SLOW_DF = 1.0f;
+   Class: one warp per item, a lane per root (solo roots do not run in their
+   item); order: one CTA, a stable counting sort by block scans. */
+constexpr int TRACK_ORDER_CLASSES = 6;
 
-__global__ void track_item_flag_kernel(const TrackArgs T, int* flag)
+__global__ void track_item_flag_kernel(const TrackArgs T, int* cls)
 {
 	const int item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	const int lane = threadIdx.x & 31;
@@ -1598,7 +1599,7 @@ __global__ void track_item_flag_kernel(const TrackArgs T, int* flag)
 	const RowDesc rd = T.rows[row];
 	const FieldView& F = T.fields[rd.field];
 	const int a = (item - T.item_start[row]) * 32 + lane;
-	bool slow = false;
+	int c = TRACK_ORDER_CLASSES - 1;
 	if (a < F.num_roots && !T.is_solo[rd.base + a])
 	{
 		const double2 z = T.master[rd.base + a];
@@ -1606,27 +1607,34 @@ __global__ void track_item_flag_kernel(const TrackArgs T, int* flag)
 		if (leaf >= 0)
 		{
 			const float2 d = eval_df32(F, leaf, z, make_double2(0, 0));
-			slow = hypotf(d.x, d.y) * (float)F.theta < TRACK_SLOW_DF;
+			const float x = hypotf(d.x, d.y) * (float)F.theta;
+			c = x < 0.03f ? 0 : x < 0.1f ? 1 : x < 0.3f ? 2 : x < 1.f ? 3 : x < 3.f ? 4 : 5;
 		}
 	}
-	const bool any = __any_sync(0xffffffffu, slow);
-	if (lane == 0) flag[item] = any ? 0 : 1;   /* 0: first */
+	c = (int)__reduce_min_sync(0xffffffffu, (unsigned)c);
+	if (lane == 0) cls[item] = c;
 }
 
-__global__ void __launch_bounds__(1024) track_item_order_kernel(int n, int* flag, int* rank, int* order)
+__global__ void __launch_bounds__(1024) track_item_order_kernel(int n, const int* cls, int* flag, int* rank, int* order)
 {
-	/* rank = exclusive scan of flag (the fast items before each item) */
-	const int fast = block_exclusive_scan(flag, rank, n);
-	const int nslow = n - fast;
-	for (int i = threadIdx.x; i < n; i += blockDim.x)
-		order[flag[i] ? nslow + rank[i] : i - rank[i]] = i;
+	int base = 0;
+	for (int c = 0; c < TRACK_ORDER_CLASSES; c++)
+	{
+		for (int i = threadIdx.x; i < n; i += blockDim.x) flag[i] = cls[i] == c;
+		__syncthreads();
+		const int cnt = block_exclusive_scan(flag, rank, n);
+		for (int i = threadIdx.x; i < n; i += blockDim.x)
+			if (flag[i]) order[base + rank[i]] = i;
+		__syncthreads();
+		base += cnt;
+	}
 }
 
 cudaError_t launch_track_item_order(cudaStream_t s, const TrackArgs& a, int* work, int* order)
 {
 	if (a.num_items == 0) return cudaSuccess;
 	track_item_flag_kernel<<<(a.num_items + 3) / 4, 128, 0, s>>>(a, work);
-	track_item_order_kernel<<<1, 1024, 0, s>>>(a.num_items, work, work + a.num_items, order);
+	track_item_order_kernel<<<1, 1024, 0, s>>>(a.num_items, work, work + a.num_items, work + 2 * (size_t)a.num_items, order);
 	return cudaGetLastError();
 }
 
