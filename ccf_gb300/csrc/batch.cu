@@ -70,9 +70,6 @@ ccf_status Engine::flush_uploads(UploadPack& up)
 	return CCF_OK;
 }
 
-/* stars per field up to which a field's setup runs in one CTA */
-constexpr int BATCH_SETUP_MAX_STARS = 8192;
-
 /* a field with generated stars, or stars the caller set, of at most
    BATCH_SETUP_MAX_STARS (a star file is read only by the per-field path) */
 bool batch_setup_fits(const Field& f)
@@ -317,7 +314,7 @@ ccf_status Engine::prepare_batch(std::vector<Field*>& fields, int verbose)
 		ccf_status rc;
 		if (alone[i])
 		{
-			rc = build_tree(f);
+			rc = build_tree(f, false);
 			if (rc == CCF_OK) rc = build_fmm(f);
 		}
 		else

@@ -384,7 +384,8 @@ ccf_status Engine::setup_outputs(Field& f)
 	   per split level), FMM (upward per level, downward from level 2, leaf
 	   flags, scan, leaf records) */
 	const int lv = info.tree_levels;
-	info.kernel_launches = (d.star_input ? 0 : 1) + 1 + (p.precision == CCF_PRECISION_MIXED ? 2 : 0) + 1 + (lv + 1) + 4 * lv
+	const int tree_launches = f.tree_one_cta ? 1 : 1 + (lv + 1) + 4 * lv;
+	info.kernel_launches = (d.star_input ? 0 : 1) + 1 + (p.precision == CCF_PRECISION_MIXED ? 2 : 0) + tree_launches
 		+ (lv + 1) + std::max(0, lv - 1) + 3;
 	return CCF_OK;
 }
@@ -415,7 +416,7 @@ cudaError_t Engine::tree_capacity(Field& f, int cap, int keep)
 	}
 }
 
-ccf_status Engine::build_tree(Field& f)
+ccf_status Engine::build_tree(Field& f, bool one_cta)
 {
 	cudaStream_t s = stream;
 	const int N = f.d.num_stars;
@@ -424,6 +425,52 @@ ccf_status Engine::build_tree(Field& f)
 	auto alloc_nodes = [&](int cap, int keep) -> cudaError_t { return tree_capacity(f, cap, keep); };
 	int cap = std::max(1024, 2 * N + 64);
 	if (f.node_cap < cap) CCF_TRY(alloc_nodes(cap, 0), "cudaMalloc(tree)");
+	f.tree_one_cta = false;
+	/* CCF_GB300_TREE_LEVELS=1 keeps the per-level build (the tests compare the two) */
+	static const bool per_level = [] {
+		const char* e = std::getenv("CCF_GB300_TREE_LEVELS");
+		return e && std::atoi(e) == 1;
+	}();
+	if (one_cta && !per_level && N <= BATCH_SETUP_MAX_STARS)
+	{
+		/* the whole tree in one CTA (tree_batch_kernel): the same tree as the
+		   per-level launches below, without their host round trip per level;
+		   a tree that outgrows the node capacity is built by those */
+		BatchSeg g;
+		std::memset(&g, 0, sizeof(g));
+		g.n = N;
+		g.pos = f.star_pos.ptr;
+		g.mass = f.star_mass.ptr;
+		g.tpos = f.star_tmp_pos.ptr;
+		g.tmass = f.star_tmp_mass.ptr;
+		g.T = f.tree_dev();
+		g.node_cap = f.node_cap;
+		g.limit = leaf_limit(f.params);
+		g.root_half = rhl;
+		CCF_TRY(batch_segs.ensure(1), "cudaMalloc(tree)");
+		CCF_TRY(batch_info.ensure(BATCH_INFO_INTS), "cudaMalloc(tree)");
+		g.info = batch_info.ptr;
+		CCF_TRY(cudaMemcpyAsync(batch_segs.ptr, &g, sizeof(g), cudaMemcpyHostToDevice, s), "upload(tree)");
+		launch_tree_batch(s, batch_segs.ptr, 1);
+		CCF_TRY(cudaGetLastError(), "tree_batch_kernel");
+		std::vector<int> fi(BATCH_INFO_INTS);
+		CCF_TRY(cudaMemcpyAsync(fi.data(), batch_info.ptr, fi.size() * sizeof(int), cudaMemcpyDeviceToHost, s), "tree");
+		CCF_TRY(cudaStreamSynchronize(s), "tree");
+		if (fi[2] & 1) { error = "Error. Tree neighbour list overflow."; return CCF_ERR_NUMERIC; }
+		if (!(fi[2] & 2))
+		{
+			const int levels = fi[0];
+			f.level_start.assign(fi.begin() + 3, fi.begin() + 3 + levels + 1);
+			f.level_count.assign(fi.begin() + 3 + TREE_MAX_LEVELS + 1, fi.begin() + 3 + TREE_MAX_LEVELS + 1 + levels + 1);
+			f.num_nodes = fi[1];
+			f.info.leaf_max_stars = g.limit;
+			f.tree_one_cta = true;
+			/* the per-level path's error word, read by build_fmm */
+			CCF_TRY(f.level_out.ensure(4), "cudaMalloc(tree)");
+			CCF_TRY(cudaMemsetAsync(f.level_out.ptr, 0, 4 * sizeof(int), s), "memset");
+			return CCF_OK;
+		}
+	}
 	CCF_TRY(f.level_out.ensure(4), "cudaMalloc(tree)");
 	f.level_start.assign(1, 0);
 	f.level_count.assign(1, 1);

@@ -143,6 +143,7 @@ struct Field
 	DBuf<int> level_out;   /* [max, nflag, err] */
 	int node_cap = 0;
 	int num_nodes = 0;
+	bool tree_one_cta = false;   /* the last tree was built by tree_batch_kernel */
 	std::vector<int> level_start, level_count;
 
 	/* FMM and leaves */
@@ -248,6 +249,10 @@ struct UploadPack
 		if (_e != cudaSuccess) return cuda_fail(_e, what); \
 	} while (0)
 
+/* stars per field up to which a field's tree (and, in a batch, its whole
+   setup) is built by one CTA (batch.cu) */
+constexpr int BATCH_SETUP_MAX_STARS = 8192;
+
 /* the root's half length (include/ccf.cuh:746) and the leaf limit: the
    reference's 32 unless leaf_max_stars lowers it */
 inline double root_half_length(const Derived& d)
@@ -281,7 +286,7 @@ private:
 	ccf_status prepare_fields(std::vector<Field*>& fields, int verbose);
 	ccf_status prepare_fields_each(std::vector<Field*>& fields, int verbose);
 	ccf_status prepare_field(Field& f, int verbose);
-	ccf_status build_tree(Field& f);
+	ccf_status build_tree(Field& f, bool one_cta = true);
 	ccf_status build_fmm(Field& f);
 	cudaError_t tree_capacity(Field& f, int cap, int keep);
 	ccf_status fmm_order(Field& f, int levels, int& P);

@@ -75,3 +75,48 @@ def test_batched_setup_launches():
     assert solo.run(-1), solo.last_error()
     # the solver's launches are shared by the batch too
     assert sum(launches) < solo.info()["kernel_launches"] + 10, launches
+
+
+_CHILD = """
+import json, sys
+import numpy as np
+from ccf_gb300 import CCF
+out = {}
+for k, cfg in enumerate(json.loads(sys.argv[1])):
+    c = CCF(**cfg)
+    c.write_mu_length_scales = 0
+    assert c.run(-1), c.last_error()
+    info = c.info()
+    out[f"info{k}"] = np.array([info[n] for n in json.loads(sys.argv[3])], dtype=np.float64)
+    out[f"stars{k}"] = c.results()["stars"]
+    out[f"fmm{k}"] = np.array([c.fmm_error()])
+np.savez(sys.argv[2], **out)
+"""
+
+
+def test_one_cta_tree_is_the_per_level_tree(tmp_path):
+    """a field of up to 8192 stars builds its tree in one CTA; the per-level
+    launches (kept for larger fields, and forced by CCF_GB300_TREE_LEVELS=1
+    in a child process) give the same tree: stars in the same order, the same
+    levels, nodes and leaves, and the same far-field error"""
+    import subprocess
+    import sys
+    cfgs = [json.loads(str(np.load(GOLDEN[0])["params"])), disc_field(1000, 4242),
+            dict(kappa_tot=0.45, kappa_star=0.35, shear=0.35, theta_star=1.0, mass_function="salpeter", m_lower=0.08,
+                 m_upper=1.5, m_solar=4.954984, rectangular=1, approx=1, num_stars=2000, num_phi=64, num_branches=32,
+                 random_seed=1235)]
+    keys = list(SAME_INFO)
+    env = dict(os.environ, CCF_GB300_TREE_LEVELS="1")
+    out = tmp_path / "levels.npz"
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", _CHILD, json.dumps(cfgs), str(out), json.dumps(keys)], env=env, cwd=root,
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lv = np.load(out)
+    for k, cfg in enumerate(cfgs):
+        c = make(cfg, "mixed")
+        assert c.run(-1), c.last_error()
+        info = c.info()
+        assert np.array_equal(np.array([info[n] for n in keys], dtype=np.float64), lv[f"info{k}"]), cfg["num_stars"]
+        assert np.array_equal(c.results()["stars"], lv[f"stars{k}"]), cfg["num_stars"]
+        assert c.fmm_error() == lv[f"fmm{k}"][0], cfg["num_stars"]
