@@ -718,21 +718,24 @@ near stars (at most 32, the stars the evaluation of f visits anyway) and
 drops the O(R + N) sums: each root walks its own row with no barrier and no
 dependence on the other roots.
 
-  * predictor: the secant through the last two accepted positions in phi;
+  * predictor: the polynomial through the last TRACK_HIST accepted positions
+    (track_predict; the secant after sub-steps);
   * corrector: z <- z - f / (f' + f S_near) until the step is below
     1e-9 theta_star (the reference's test, include/ccf_functions.cuh:385);
     a step that does not shrink by TRACK_CONTRACT, a non-finite step or
     TRACK_ITERS iterations without convergence halve the phi sub-step and
     restart from the last accepted position;
   * check: every final root of a column is entered into that column's hash
-    table of 2^-20 theta_star cells, so two roots that converged to one zero
-    are seen (the global repulsion of the full Aberth step is what keeps the
-    reference's roots apart).  A row with such a pair, a root lost after the
-    sub-step and evaluation limits, or a non-finite 1/mu bound is run again
-    from its branch-centre roots by the full-sum continuation (solve_kernel),
-    so every row written is either a verified tracked row or the reference's
-    scheme.  Rows whose results are kept report their statistics through
-    collect_rerun_kernel; re-run rows through the full-sum kernel. */
+    table of 2^-20 theta_star cells (track_check_kernel, after the launch), so
+    two roots that converged to one zero are seen (the global repulsion of
+    the full Aberth step is what keeps the reference's roots apart).  A row
+    with such a pair, a root lost after the sub-step and evaluation limits,
+    or a non-finite 1/mu bound is tracked again from its branch-centre roots
+    with sub-steps of 1/TRACK_FINE_SUB of a step, and a row failing that too
+    is run by the full-sum continuation (solve_kernel), so every row written
+    is either a verified tracked row or the reference's scheme.  Rows whose
+    results are kept report their statistics through collect_rerun_kernel;
+    re-run rows through the full-sum kernel. */
 
 constexpr int TNT = 128;                 /* threads per CTA of the tracker */
 constexpr int TSUB = TRACK_TSUB;         /* one phi step in sub-step units */
