@@ -471,61 +471,60 @@ CCF_D double fold_tail(const double2* __restrict__ e, int n, double2 z0, double 
 	return t;
 }
 
-__global__ void fold_smooth_kernel(int num_leaves, int P, const double2* __restrict__ leaf_center,
+/* one leaf per CTA of three warps: warp 0 folds the alpha series (eq) into
+   block 0, warp 1 the d alpha / d zbar series (ef) into block 1, warp 2 the
+   d2 alpha / d zbar2 series (er) into block 2; each lane forms one shifted
+   coefficient and a share of its series' tail beyond the block's order, and
+   the leaf folds when all three tails are negligible */
+__global__ void __launch_bounds__(96) fold_smooth_kernel(int num_leaves, int P, const double2* __restrict__ leaf_center,
 	const double* __restrict__ leaf_inv_half, const double2* __restrict__ loc, const double2* __restrict__ ef, int nf,
 	const double2* __restrict__ er, int nr, const double2* __restrict__ eq, int nq, double radius,
 	float4* __restrict__ loc_df, float2* __restrict__ loc3f, double2* __restrict__ loc64, unsigned char* __restrict__ fold)
 {
 	__shared__ double inv[FOLD_MAXD + 1];
+	__shared__ int s_ok[3];
 	for (int k = threadIdx.x; k <= FOLD_MAXD; k += blockDim.x) inv[k] = k ? 1.0 / k : 0.0;
 	__syncthreads();
-	const int lane = threadIdx.x & 31;
-	const int l = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-	if (l >= num_leaves) return;
+	const int lane = threadIdx.x & 31, part = threadIdx.x >> 5;
+	const int l = blockIdx.x;
+	if (l >= num_leaves) return;   /* block-uniform */
 	const double2 c = leaf_center[l];
 	const double h = 1.0 / leaf_inv_half[l];
 	if (hypot(c.x, c.y) + 1.4142135623730951 * h > radius || nf > FOLD_MAXD || nr > FOLD_MAXD || nq > FOLD_MAXD)
 	{
-		if (lane == 0) fold[l] = 0;
+		if (threadIdx.x == 0) fold[l] = 0;
 		return;
 	}
 	/* block 0 (alpha) gains dz^0 .. dz^(P-1) of eq at its coefficients 1 .. P,
-	   block 1 (f's alpha'' block) dz^0 .. dz^(P-2) of ef at 2 .. P, block 2
-	   (f''s alpha''' block) dz^0 .. dz^(P-3) of er at 3 .. P */
+	   block 1 (the d alpha / d zbar block) dz^0 .. dz^(P-2) of ef at 2 .. P,
+	   block 2 (the d2 alpha / d zbar2 block) dz^0 .. dz^(P-3) of er at 3 .. P */
+	const double2* e = part == 0 ? eq : part == 1 ? ef : er;
+	const int n = part == 0 ? nq : part == 1 ? nf : nr;
 	const int i = lane;
-	const double2 q = i >= 1 && i <= P ? fold_coef(eq, nq, c, h, i - 1, inv) : make_double2(0, 0);
-	const double2 pf = i >= 2 && i <= P ? fold_coef(ef, nf, c, h, i - 2, inv) : make_double2(0, 0);
-	const double2 r = i >= 3 && i <= P ? fold_coef(er, nr, c, h, i - 3, inv) : make_double2(0, 0);
-	double tq = fold_tail(eq, nq, c, h, P + lane, inv);
-	double tp = fold_tail(ef, nf, c, h, P - 1 + lane, inv);
-	double tr = fold_tail(er, nr, c, h, P - 2 + lane, inv);
-	for (int o = 16; o; o >>= 1)
-	{
-		tq += __shfl_xor_sync(0xffffffffu, tq, o);
-		tp += __shfl_xor_sync(0xffffffffu, tp, o);
-		tr += __shfl_xor_sync(0xffffffffu, tr, o);
-	}
+	const double2 v = i >= part + 1 && i <= P ? fold_coef(e, n, c, h, i - part - 1, inv) : make_double2(0, 0);
+	double t = fold_tail(e, n, c, h, P - part + lane, inv);
+	for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
 	const double tol = 1e-15;
-	const bool ok = tq <= tol && tp <= tol && tr <= tol;
-	if (lane == 0) fold[l] = ok ? 1 : 0;
+	if (lane == 0) s_ok[part] = t <= tol ? 1 : 0;
+	__syncthreads();
+	const bool ok = s_ok[0] && s_ok[1] && s_ok[2];
+	if (threadIdx.x == 0) fold[l] = ok ? 1 : 0;
 	if (!ok || i > P) return;
 	auto split = [](double x) {
 		float hi = __double2float_rn(x);
 		return make_float2(hi, __double2float_rn(x - (double)hi));
 	};
-	const double2 a0 = cadd(loc[((size_t)l * 3 + 0) * (P + 1) + i], q);
-	const double2 a1 = cadd(loc[((size_t)l * 3 + 1) * (P + 1) + i], pf);
-	const double2 a2 = cadd(loc[((size_t)l * 3 + 2) * (P + 1) + i], r);
-	const float2 x0 = split(a0.x), y0 = split(a0.y), x1 = split(a1.x), y1 = split(a1.y);
-	loc_df[((size_t)l * 2 + 0) * (P + 1) + i] = make_float4(x0.x, y0.x, x0.y, y0.y);
-	loc_df[((size_t)l * 2 + 1) * (P + 1) + i] = make_float4(x1.x, y1.x, x1.y, y1.y);
-	loc3f[(size_t)l * (P + 1) + i] = make_float2((float)a2.x, (float)a2.y);
-	if (loc64)
+	const double2 a = cadd(loc[((size_t)l * 3 + part) * (P + 1) + i], v);
+	if (part < 2)
 	{
-		loc64[((size_t)l * 3 + 0) * (P + 1) + i] = a0;
-		loc64[((size_t)l * 3 + 1) * (P + 1) + i] = a1;
-		loc64[((size_t)l * 3 + 2) * (P + 1) + i] = a2;
+		const float2 x = split(a.x), y = split(a.y);
+		loc_df[((size_t)l * 2 + part) * (P + 1) + i] = make_float4(x.x, y.x, x.y, y.y);
 	}
+	else
+	{
+		loc3f[(size_t)l * (P + 1) + i] = make_float2((float)a.x, (float)a.y);
+	}
+	if (loc64) loc64[((size_t)l * 3 + part) * (P + 1) + i] = a;
 }
 
 void launch_fold_smooth(cudaStream_t s, int num_leaves, int P, const double2* leaf_center, const double* leaf_inv_half,
@@ -533,9 +532,8 @@ void launch_fold_smooth(cudaStream_t s, int num_leaves, int P, const double2* le
 	float4* loc_df, float2* loc3f, double2* loc64, unsigned char* fold)
 {
 	if (num_leaves <= 0) return;
-	const int warps = 4;
-	fold_smooth_kernel<<<(num_leaves + warps - 1) / warps, warps * 32, 0, s>>>(num_leaves, P, leaf_center, leaf_inv_half, loc, ef, nf, er,
-		nr, eq, nq, radius, loc_df, loc3f, loc64, fold);
+	fold_smooth_kernel<<<num_leaves, 96, 0, s>>>(num_leaves, P, leaf_center, leaf_inv_half, loc, ef, nf, er, nr, eq, nq,
+		radius, loc_df, loc3f, loc64, fold);
 }
 
 } /* namespace ccf */
