@@ -138,15 +138,19 @@ __global__ void fmm_upward_kernel(TreeDev T, int start, int count, int P, const 
    handed round by shuffles; lane p takes t^p from a product scan; and the
    M2L sum over k is a binomial-weighted sum of the pre-scaled b_k t^k (two
    FMAs a term) instead of a complex Horner recurrence. */
-CCF_D void fmm_downward_node(const TreeDev& T, int n, int P, int p, const double2* __restrict__ pos,
-	const double* __restrict__ mass, const double2* __restrict__ multi, double2* __restrict__ local,
+/* part `part` of nparts of node n's downward coefficients, one warp: the
+   L2L in part 0, the M2L sources j = part, part + nparts, ..., the P2L
+   sources likewise; fmm_downward_reduce sums the parts in their order */
+constexpr int DOWN_PARTS = 4;
+CCF_D double2 fmm_downward_part(const TreeDev& T, int n, int P, int p, int part, int nparts, const double2* __restrict__ pos,
+	const double* __restrict__ mass, const double2* __restrict__ multi, const double2* __restrict__ local,
 	const double* __restrict__ B)
 {
 	const bool act = p <= P;
 	double2 cn = T.center[n];
 	double2 r = make_double2(0, 0);
 	/* L2L: d_p = sum_{k>=max(p,1)} c_k C(k,p) dz^(k-p) / 2^p, dz = (c - c_parent)/h_parent */
-	if (act)
+	if (act && part == 0)
 	{
 		int par = T.parent[n];
 		const double2* cl = local + (size_t)par * (P + 1);
@@ -178,7 +182,7 @@ CCF_D void fmm_downward_node(const TreeDev& T, int n, int P, int p, const double
 		lq = make_double2(log(hypot(dz.x, dz.y)), atan2(-dz.y, -dz.x));
 		hq = log(hf);
 	}
-	for (int j = 0; j < nm; j++)
+	for (int j = part; j < nm; j += nparts)
 	{
 		const int f = __shfl_sync(0xffffffffu, fq, j);
 		const double2 t = shfl_c(tq, j);
@@ -212,7 +216,7 @@ CCF_D void fmm_downward_node(const TreeDev& T, int n, int P, int p, const double
 	double ihn = 1.0 / hn;
 	double lhn = log(hn);
 	const double ip = p > 0 ? 1.0 / p : 0.0;
-	for (int j = 0; j < np; j++)
+	for (int j = part; j < np; j += nparts)
 	{
 		int f = T.p2l[n * MAX_P2L + j];
 		int s = T.star_start[f], ns = T.star_count[f];
@@ -249,16 +253,35 @@ CCF_D void fmm_downward_node(const TreeDev& T, int n, int P, int p, const double
 		}
 		r = cadd(r, v);
 	}
-	if (act) local[(size_t)n * (P + 1) + p] = r;
+	return r;
 }
 
-__global__ void fmm_downward_kernel(TreeDev T, int start, int count, int P, const double2* __restrict__ pos,
+/* node n's downward pass by the DOWN_PARTS warps of the calling block (every
+   thread calls it): the parts' sums meet in shared memory in a fixed order */
+CCF_D void fmm_downward_node(const TreeDev& T, int n, int P, const double2* __restrict__ pos,
 	const double* __restrict__ mass, const double2* __restrict__ multi, double2* __restrict__ local,
 	const double* __restrict__ B)
 {
-	int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-	if (w >= count) return;   /* warp-uniform */
-	fmm_downward_node(T, start + w, P, threadIdx.x & 31, pos, mass, multi, local, B);
+	__shared__ double2 red[DOWN_PARTS][32];
+	const int p = threadIdx.x & 31, part = threadIdx.x >> 5;
+	red[part][p] = fmm_downward_part(T, n, P, p, part, DOWN_PARTS, pos, mass, multi, local, B);
+	__syncthreads();
+	if (part == 0 && p <= P)
+	{
+		double2 r = red[0][p];
+		for (int k = 1; k < DOWN_PARTS; k++) r = cadd(r, red[k][p]);
+		local[(size_t)n * (P + 1) + p] = r;
+	}
+	__syncthreads();
+}
+
+/* one node per block of DOWN_PARTS warps */
+__global__ void __launch_bounds__(DOWN_PARTS * 32) fmm_downward_kernel(TreeDev T, int start, int count, int P,
+	const double2* __restrict__ pos, const double* __restrict__ mass, const double2* __restrict__ multi,
+	double2* __restrict__ local, const double* __restrict__ B)
+{
+	if ((int)blockIdx.x >= count) return;   /* block-uniform */
+	fmm_downward_node(T, start + blockIdx.x, P, pos, mass, multi, local, B);
 }
 
 /* leaf records for the solver: centre, 1/h, packed near stars (neighbours
@@ -344,8 +367,7 @@ void launch_fmm_upward(cudaStream_t s, const TreeDev& T, int start, int count, i
 void launch_fmm_downward(cudaStream_t s, const TreeDev& T, int start, int count, int P, const double2* pos, const double* mass,
 	const double2* multi, double2* local, const double* B)
 {
-	long long threads = (long long)count * 32;
-	fmm_downward_kernel<<<(int)((threads + 127) / 128), 128, 0, s>>>(T, start, count, P, pos, mass, multi, local, B);
+	if (count > 0) fmm_downward_kernel<<<count, DOWN_PARTS * 32, 0, s>>>(T, start, count, P, pos, mass, multi, local, B);
 }
 void launch_leaf_build(cudaStream_t s, const TreeDev& T, int num_nodes, const int* leaf_index, int P, double theta2,
 	const double2* pos, const double* mass, const double2* local, double2* leaf_center, double* leaf_inv_half,
@@ -561,12 +583,20 @@ __global__ void fmm_zero_batch_kernel(const BatchSeg* __restrict__ segs)
 __global__ void fmm_level_batch_kernel(const BatchSeg* __restrict__ segs, int L, int upward)
 {
 	const BatchSeg& S = segs[blockIdx.y];
-	if (L > S.info[0]) return;
-	const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-	if (w >= S.info[3 + TREE_MAX_LEVELS + 1 + L]) return;   /* warp-uniform */
-	const int n = S.info[3 + L] + w;
-	if (upward) fmm_upward_node(S.T, n, S.P, threadIdx.x & 31, S.pos, S.mass, S.multi, S.B);
-	else fmm_downward_node(S.T, n, S.P, threadIdx.x & 31, S.pos, S.mass, S.multi, S.local, S.B);
+	if (L > S.info[0]) return;   /* block-uniform */
+	if (upward)
+	{
+		/* four nodes per block, one warp each */
+		const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+		if (w >= S.info[3 + TREE_MAX_LEVELS + 1 + L]) return;   /* warp-uniform */
+		fmm_upward_node(S.T, S.info[3 + L] + w, S.P, threadIdx.x & 31, S.pos, S.mass, S.multi, S.B);
+	}
+	else
+	{
+		/* one node per block, DOWN_PARTS warps */
+		if ((int)blockIdx.x >= S.info[3 + TREE_MAX_LEVELS + 1 + L]) return;   /* block-uniform */
+		fmm_downward_node(S.T, S.info[3 + L] + blockIdx.x, S.P, S.pos, S.mass, S.multi, S.local, S.B);
+	}
 }
 
 __global__ void __launch_bounds__(1024) leaf_number_batch_kernel(const BatchSeg* __restrict__ segs)
@@ -633,7 +663,9 @@ void launch_fmm_batch(cudaStream_t s, const BatchSeg* segs, int nseg, int max_le
 	fmm_zero_batch_kernel<<<dim3(std::max(gz, 1), nseg), 256, 0, s>>>(segs);
 	const int gx = std::max(1, (max_level_nodes + 3) / 4);
 	for (int L = max_levels; L >= 0; L--) fmm_level_batch_kernel<<<dim3(gx, nseg), 128, 0, s>>>(segs, L, 1);
-	for (int L = 2; L <= max_levels; L++) fmm_level_batch_kernel<<<dim3(gx, nseg), 128, 0, s>>>(segs, L, 0);
+	static_assert(DOWN_PARTS * 32 == 128, "the level kernel's blocks");
+	for (int L = 2; L <= max_levels; L++)
+		fmm_level_batch_kernel<<<dim3(std::max(1, max_level_nodes), nseg), 128, 0, s>>>(segs, L, 0);
 	leaf_number_batch_kernel<<<nseg, 1024, 0, s>>>(segs);
 }
 void launch_leaf_batch(cudaStream_t s, const BatchSeg* segs, int nseg)
