@@ -966,7 +966,8 @@ ccf_status Engine::solve(std::vector<Field*>& fields, int verbose)
 	/* every field's seeds in one launch */
 	CCF_TRY(P.seeds.ensure(seeds.size()), "cudaMalloc(seeds)");
 	CCF_TRY(cudaMemcpyAsync(P.seeds.ptr, seeds.data(), seeds.size() * sizeof(SeedSeg), cudaMemcpyHostToDevice, s), "upload");
-	launch_seed_roots_batch(s, P.seeds.ptr, (int)seeds.size(), max_seeds);
+	for (size_t i0 = 0; i0 < seeds.size(); i0 += 65535)   /* blockIdx.y is the field */
+		launch_seed_roots_batch(s, P.seeds.ptr + i0, (int)std::min<size_t>(65535, seeds.size() - i0), max_seeds);
 	CCF_TRY(cudaGetLastError(), "seed_roots_batch_kernel");
 	/* largest rows first */
 	auto order = [](std::vector<RowDesc>& rows, std::vector<double>& cost) {
@@ -1247,8 +1248,13 @@ ccf_status Engine::prepare_fields(std::vector<Field*>& fields, int verbose)
 		for (Field* f : fields) (batch_setup_fits(*f) ? small : rest).push_back(f);
 		if (small.size() >= 2)
 		{
-			ccf_status rc = prepare_batch(small, verbose);
-			if (rc != CCF_OK) return rc;
+			/* the batched launches index fields by blockIdx.y: at most 65535 a launch */
+			for (size_t i0 = 0; i0 < small.size(); i0 += 65535)
+			{
+				std::vector<Field*> part(small.begin() + i0, small.begin() + std::min(small.size(), i0 + 65535));
+				ccf_status rc = part.size() >= 2 ? prepare_batch(part, verbose) : prepare_fields_each(part, verbose);
+				if (rc != CCF_OK) return rc;
+			}
 			if (rest.empty()) return CCF_OK;
 			return prepare_fields_each(rest, verbose);
 		}
