@@ -75,3 +75,23 @@ def test_clock_summary_parses_samples_and_reasons():
     assert s["sm_mhz"] == (2070.0 + 1980.0) / 2
     assert s["reasons"] == ["sw_power_cap"]
     assert bench.ClockSampler(0).summary() == {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+
+
+def test_continuation_roofline_record():
+    """the bench's roofline record for the headline field's counts: the §8(d)
+    algorithmic work over the continuation's span against the FP32 peak, the
+    FP64 share beside it, the executed double-float operations per flop and
+    the DRAM bytes scaled from the full-size capture"""
+    info = dict(HEADLINE_INFO, leaves_folded=1061, num_roots=4056, root_updates=10206621, root_updates_init=641077,
+                sum_terms=3095830675, sum_terms_init=3095830675)
+    peaks = {"fp32_tflops": 78.477, "fp64_tflops": 1.2545}
+    r = bench.continuation_roofline(info, 1, 0.00891, peaks, 2048)
+    assert r["bound"] == "fp32" and r["unit"] == "TFLOP/s" and r["peak"] == 78.477
+    evals = 10206621 - 641077
+    flops = bench.algorithmic_flops_per_eval(info, 1) * evals
+    assert math.isclose(r["achieved"], flops / 0.00891 / 1e12)
+    assert math.isclose(r["frac"], r["achieved"] / 78.477)
+    assert math.isclose(r["frac_of_fp64_peak"], r["achieved"] / 1.2545)
+    assert 1.0 < r["achieved"] < 1.3
+    assert 5.0 < r["executed_ops"]["per_algorithmic_flop"] < 6.0
+    assert math.isclose(r["traffic"], bench.CONT_DRAM_BYTES_PER_POINT * 4056 * 2048)
