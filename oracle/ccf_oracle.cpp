@@ -1404,14 +1404,30 @@ int oracle_run(const oracle_params* p, oracle_info* info, double* stars_out,
 	std::vector<char> fin((size_t)nb * 2 * nroots, 0);
 	auto center_row = [&](int c) { return (size_t)(half + c * nphi / nb + c); };   /* ccf_functions.cuh:373 */
 
-	/* include/ccf.cuh:711-726 */
+	/* include/ccf.cuh:711-726; or (seed_curves) the two zeros of f for the
+	   star alone at the centre's phase, theta^2 m / (z - z_i)^2 = a e^{-i phi}
+	   - gamma with a = 1 - kappa_tot + kappa_star */
 	for (int c = 0; c < nb; c++)
 	{
 		Cx* row = &z[center_row(c) * nroots];
+		const double phi = center_phi(c, nb);
+		const double a_lin = 1 - F.kappa_tot + F.kappa_star;
+		const double dx = a_lin * std::cos(phi) - F.shear, dy = -a_lin * std::sin(phi);
+		const double rd = std::hypot(dx, dy), half_arg = -0.5 * std::atan2(dy, dx);
 		for (int i = 0; i < nstars; i++)
 		{
-			row[i] = addr(R.stars_gen[i].pos, 1);
-			row[i + nstars] = subr(R.stars_gen[i].pos, 1);
+			if (p->seed_curves && rd > 1e-6 && R.stars_gen[i].mass > 0)
+			{
+				const double r = F.theta * std::sqrt(R.stars_gen[i].mass / rd);
+				const Cx w = cx(r * std::cos(half_arg), r * std::sin(half_arg));
+				row[i] = add(R.stars_gen[i].pos, w);
+				row[i + nstars] = sub(R.stars_gen[i].pos, w);
+			}
+			else
+			{
+				row[i] = addr(R.stars_gen[i].pos, 1);
+				row[i + nstars] = subr(R.stars_gen[i].pos, 1);
+			}
 		}
 		int extra = nroots - 2 * nstars;
 		for (int i = 0; i < extra; i++)

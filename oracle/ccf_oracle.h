@@ -76,6 +76,10 @@ typedef struct oracle_params
 	                         0: the reference's in-place order, rows split over
 	                         the threads.  Both converge to the zeros of f; the
 	                         order of the updates only changes the path. */
+	int seed_curves;      /* 1: the branch centres' seeds on each star's own
+	                         critical curve, z_i +/- theta sqrt(m) / sqrt(a e^{-i phi}
+	                         - gamma) (the CUDA path's seeds), instead of the
+	                         reference's z_i +/- 1 */
 } oracle_params;
 
 typedef struct oracle_info

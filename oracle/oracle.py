@@ -57,6 +57,7 @@ class OracleParams(ctypes.Structure):
         ("branch_stride", ctypes.c_int),
         ("polish_newton", ctypes.c_int),
         ("jacobi", ctypes.c_int),
+        ("seed_curves", ctypes.c_int),
     ]
 
 
